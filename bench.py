@@ -1,0 +1,407 @@
+"""Benchmark: TOD samples/s of the polarized-beam convolution on one GB300.
+
+Workload (the production-size plain forward): sky HEALPix nside 1024 float32
+I,Q,U (seeded C_ell ~ ell^-2 Gaussian random fields, V = 0); beam nside 2048,
+radius 3 deg, elliptical Gaussian FWHM 1.5 deg, ellipticity 0.05, epsilon
+0.01; one detector pair; 2,000,000 samples of a constant-elevation sweep
+(RA += 360/4096 deg per sample, Dec += 0.05 deg per sweep from -80 deg, psi
+uniform); FP64 pointing, FP32 sky and beam.  Synthetic, seeded.
+
+One step = one TUNED forward over all samples with the inputs resident in HBM
+(`value`); L2 is flushed (a 256 MiB write) between timed steps.  `e2e` is
+the same metric through the C ABI with host buffers: pinned host pointing is
+copied in (pisco_set_scan), the forward runs and the TOD comes back
+(pisco_forward), every step.  Also reported: the PLAIN form on a bounded
+prefix, the rms error of TUNED against the FP64 form, the roofline of the
+forward kernel and the CPU baseline (oracle/_ref when it loads on this
+host, else the oracle's C restatement) on a bounded prefix.
+
+`--impl reference` times the reference's CPU implementation of the path
+(oracle/_ref: the reference Convolver compiled from its own sources, when it
+was built for this host; else the oracle port) with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "c2_nside1024_beam3deg_2Msamples_sweep"
+METRIC = "TOD samples/s (nside 1024 sky, 3 deg beam, tuned FP32/FP64-pointing forward)"
+BYTES_PER_PAIR = 48     # sky IQUV f32 + beam a IQUV f32 + beam b IQUV f32
+BYTES_PER_SAMPLE = 32   # 3 x 8 B FP64 pointing in + 2 x 4 B FP32 TOD out
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:  # noqa: BLE001
+        return os.cpu_count() or 1
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per launch of the tuned forward from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "tuned_forward_c2.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_full_c2")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:  # noqa: BLE001
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:  # noqa: BLE001
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(device: str, nsamples: int):
+    from pisco4cmb_gb300 import PolBeam, beam_npix_for_radius, synth
+
+    w = synth.WORKLOADS[2]
+    t0 = time.time()
+    sky = synth.grf_sky(w["nside_sky"], 2, dtype=np.float32, device=device)
+    nsb = w["nside_beam"]
+    npb = beam_npix_for_radius(nsb, math.radians(w["radius_deg"]))
+    beam = PolBeam(nsb, npb, w["epsilon"], "p")
+    fx, fy = synth.elliptical_fwhm(w["fwhm_deg"], w["ellipticity"])
+    beam.make_unpol_gaussian_elliptical_beams(fx, fy, 0.0)
+    beam.build(w["nside_sky"])
+    ra, dec, psi = synth.sweep_scan(nsamples, 2)
+    return dict(sky=sky, beam=beam, ra=ra, dec=dec, pa=psi, nside_sky=w["nside_sky"],
+                gen_s=time.time() - t0)
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_forward(wl, n: int, threads: int, prefer_ref: bool = True):
+    """(kind, seconds, tod_a) of the CPU implementation on the first n samples."""
+    import oracle
+
+    oracle.build_oracle()
+    ba, bb = wl["beam"].planes()
+    ra, dec, pa = (wl[k][:n] for k in ("ra", "dec", "pa"))
+    use_ref = False
+    if prefer_ref and oracle.ref_available():
+        try:
+            oracle.ref_lib()
+            use_ref = True
+        except OSError:
+            use_ref = False
+    t0 = time.perf_counter()
+    if use_ref:
+        a, _ = oracle.ref_convolve(ra, dec, pa, wl["nside_sky"], wl["sky"], wl["beam"].nside,
+                                   ba, bb, nthreads=threads)
+    else:
+        a, _ = oracle.convolve_f32(ra, dec, pa, wl["nside_sky"], wl["sky"], wl["beam"].nside,
+                                   ba, bb, nthreads=threads)
+    return ("reference" if use_ref else "port"), time.perf_counter() - t0, a
+
+
+def cpu_sample_size(wl, threads: int, target_s: float):
+    kind, t, _ = cpu_forward(wl, 256, threads)
+    per = t / 256
+    return max(256, min(len(wl["ra"]), int(target_s / max(per, 1e-9)))), kind
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    wl = make_workload("cpu", 200_000)
+    threads = host_cores()
+    n, kind = cpu_sample_size(wl, threads, 5.0)
+    for _ in range(args.warmup):
+        cpu_forward(wl, min(n, 2048), threads)
+    times = []
+    for _ in range(args.steps):
+        _, t, _ = cpu_forward(wl, n, threads)
+        times.append(t)
+    t_step = sum(times) / len(times)
+    v = n / t_step
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded GRF sky, Gaussian beam, sweep scan)",
+            "config": {"workload": WORKLOAD, "sample": "first %d of 2,000,000 sweep samples" % n,
+                       "parallelism": "host OpenMP, %d threads" % threads},
+            "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": kind,
+                             "sample": "first %d samples of the workload" % n},
+            "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu_arm(args, rank, world, local):
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, RunConfig, Scan, Sky
+
+    torch.cuda.set_device(local)
+    dev = "cuda:%d" % local
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(dev))
+    wl = make_workload(dev, args.samples)
+    n = len(wl["ra"])
+    sky = wl["sky"]
+    conv = GPUConvolver(RunConfig(deviceId=local, ptgPerConv=1 << 22), form="tuned")
+    conv.update_sky(Sky(wl["nside_sky"], sky[0], sky[1], sky[2], None))
+    conv.update_beam(wl["beam"])
+    conv.update_scan(Scan(n, wl["ra"], wl["dec"], wl["pa"]))
+    pairs = conv.count_pairs()
+
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    out_a = torch.empty(n, dtype=torch.float32, device=dev)
+    out_b = torch.empty(n, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(form="tuned", m=None):
+        conv.forward_device(out_a.data_ptr(), out_b.data_ptr(), n=m or n, stream=sh, form=form)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    conv.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.fill_(i & 0xff)
+                evs[i][0].record(stream)
+                step()
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+    conv.sync()
+    kernel_ms = [s.elapsed_time(e) for s, e in evs]
+    t_total = sum(kernel_ms) / 1e3
+    if dist:
+        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        t_total = float(t.item())
+    ms_step = t_total / args.steps * 1e3
+    value = n * world * args.steps / t_total
+    fallbacks = conv.last_fallbacks()
+
+    # plain form on a bounded prefix (it is FP64-per-pair and slow on GB300)
+    m_plain = min(n, args.plain_samples)
+    with torch.cuda.stream(stream):
+        step("plain", m_plain)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step("plain", m_plain)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    plain_sps = m_plain / (e0.elapsed_time(e1) / 1e3)
+
+    # accuracy of TUNED vs FP64 on a bounded prefix (untimed)
+    m_acc = min(n, args.accuracy_samples)
+    ta = torch.empty(m_acc, dtype=torch.float64, device=dev)
+    tb = torch.empty(m_acc, dtype=torch.float64, device=dev)
+    fa = torch.empty(m_acc, dtype=torch.float64, device=dev)
+    fb = torch.empty(m_acc, dtype=torch.float64, device=dev)
+    conv.forward_device(ta.data_ptr(), tb.data_ptr(), out_f64=True, n=m_acc, form="tuned")
+    conv.forward_device(fa.data_ptr(), fb.data_ptr(), out_f64=True, n=m_acc, form="fp64")
+    conv.sync()
+    rms = torch.sqrt(torch.mean(torch.cat([fa, fb]) ** 2)).item()
+    err = torch.cat([ta - fa, tb - fb])
+    rms_err = torch.sqrt(torch.mean(err ** 2)).item() / rms
+    max_err = torch.max(torch.abs(err)).item() / rms
+
+    # e2e through the C ABI with pinned host buffers, host<->device copies inside
+    ra_h = torch.from_numpy(wl["ra"]).pin_memory()
+    dec_h = torch.from_numpy(wl["dec"]).pin_memory()
+    pa_h = torch.from_numpy(wl["pa"]).pin_memory()
+    a_h = torch.empty(n, dtype=torch.float32).pin_memory()
+    b_h = torch.empty(n, dtype=torch.float32).pin_memory()
+    import ctypes
+
+    from pisco4cmb_gb300 import _lib
+
+    L = _lib.load()
+
+    def e2e_step():
+        _lib.check(L.pisco_set_scan(conv.ctx, n, ctypes.c_void_p(ra_h.data_ptr()),
+                                    ctypes.c_void_p(dec_h.data_ptr()),
+                                    ctypes.c_void_p(pa_h.data_ptr()), _lib.FLOAT64), conv.ctx, "set_scan")
+        _lib.check(L.pisco_forward(conv.ctx, b"p", ctypes.c_void_p(a_h.data_ptr()),
+                                   ctypes.c_void_p(b_h.data_ptr()), _lib.FLOAT32, _lib.FORM_TUNED),
+                   conv.ctx, "forward")
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e2e_t = 0.0
+    for i in range(args.steps):
+        flush.fill_(i & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t += time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = n * world * args.steps / e2e_t
+    assert np.allclose(a_h.numpy()[:1000], out_a.cpu().numpy()[:1000], rtol=1e-6, atol=1e-4)
+
+    # roofline of the forward kernel (algorithmic bytes per launch / launch time)
+    peak, peak_kind = measured_peaks()
+    alg_bytes = pairs * BYTES_PER_PAIR + n * BYTES_PER_SAMPLE
+    achieved = alg_bytes / (t_total / args.steps) / 1e9
+    traffic = ncu_traffic_per_launch()
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            threads = host_cores()
+            wl_cpu = dict(wl)
+            m_cpu, kind = cpu_sample_size(wl_cpu, threads, args.cpu_seconds)
+            kind, t_cpu, cpu_a = cpu_forward(wl_cpu, m_cpu, threads)
+            cpu = {"value": m_cpu / t_cpu, "unit": "samples/s", "cores": threads, "kind": kind,
+                   "sample": "first %d of the %d workload samples, %.1f s" % (m_cpu, n, t_cpu)}
+        line = {
+            "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded GRF sky C_l~l^-2, elliptical Gaussian PolBeam, sweep scan)",
+            "config": {"workload": WORKLOAD, "nsamples": n, "nside_sky": 1024, "nside_beam": 2048,
+                       "beam_radius_deg": 3.0, "pairs_per_step": pairs,
+                       "pairs_per_sample": pairs / n, "form": "tuned",
+                       "l2": "flushed between timed steps (256 MiB write); sky 201 MB > L2",
+                       "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": n * 24,
+                    "d2h_bytes_per_step": n * 8},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic,
+                         "bytes_model": "48 B/pair x exact disc pairs + 32 B/sample"},
+            "plain": {"value": plain_sps, "unit": "samples/s", "sample": m_plain,
+                      "tuned_over_plain": value / world / plain_sps},
+            "accuracy": {"rms_err_vs_fp64": rms_err, "max_err_vs_fp64": max_err,
+                         "sample": m_acc, "relative_to": "TOD rms"},
+            "macs_per_s": pairs * 8 * world * args.steps / t_total,
+            "fp64_fallback_pairs_per_step": fallbacks,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "input_gen_s": wl["gen_s"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=2_000_000)
+    ap.add_argument("--plain-samples", type=int, default=100_000)
+    ap.add_argument("--accuracy-samples", type=int, default=50_000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    return run_gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,39 @@
+#!/bin/sh
+# Builds oracle/_ref/ (TEST INFRASTRUCTURE ONLY) from the reference's own
+# sources, read in place from the reference tree ($PISCO_REFERENCE, default
+# /root/reference).  Nothing from the reference tree is copied; outputs go to
+# oracle/_ref/ only (git-ignored).
+#   libpisco_ref.so    : Convolver, Sky, Scan, PolBeam, Sphtrigo compiled
+#                        unmodified with the reference's CPU flags
+#                        (CMakeLists.txt:27,37-39) against the HEALPix shim
+#                        in oracle/shim/ (Healpix C++ itself is absent).
+#   libpisco_refdev.so : the reference's device HEALPix port and device
+#                        rotation (cudaHealpix.cu, cudaSphtransf.cu)
+#                        compiled for the host with __device__ removed.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${PISCO_REFERENCE:-/root/reference}
+OUT="$HERE/_ref"
+CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
+if [ ! -f "$REF/src/Convolver/convolver.cpp" ]; then
+    echo "build_ref.sh: reference tree not found at $REF; skipping" >&2
+    exit 0
+fi
+mkdir -p "$OUT/obj"
+gcc -O2 -fPIC -fopenmp -ffp-contract=off -c "$HERE/oracle.c" -o "$OUT/obj/oracle.o"
+CXXF="-O3 -march=native -fopenmp -pthread -DCONVOLVER_OPENMPENABLED -fPIC -w -I$REF/src -I$HERE/shim -I$HERE"
+for f in Convolver/convolver Sky/sky Scan/scan Polbeam/polbeam Sphtrigo/sphtrigo; do
+    g++ $CXXF -c "$REF/src/$f.cpp" -o "$OUT/obj/$(basename $f).o" &
+done
+g++ $CXXF -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" &
+wait
+g++ -shared -fopenmp -o "$OUT/libpisco_ref.so" "$OUT"/obj/convolver.o "$OUT"/obj/sky.o \
+    "$OUT"/obj/scan.o "$OUT"/obj/polbeam.o "$OUT"/obj/sphtrigo.o "$OUT"/obj/ref_harness.o \
+    "$OUT"/obj/oracle.o
+DEVF="-O2 -fPIC -w -x c++ -D__device__= -include cmath -include math.h -I$REF/src -I$REF/src/GpuConvolver/cuda -I$CUDA_INC"
+g++ $DEVF -c "$REF/src/GpuConvolver/cuda/cudaHealpix.cu" -o "$OUT/obj/cudaHealpix.o"
+g++ $DEVF -c "$REF/src/GpuConvolver/cuda/cudaSphtransf.cu" -o "$OUT/obj/cudaSphtransf.o"
+g++ -O2 -fPIC -w -I$REF/src -I$CUDA_INC -D__device__= -c "$HERE/refdev_harness.cpp" -o "$OUT/obj/refdev_harness.o"
+g++ -shared -o "$OUT/libpisco_refdev.so" "$OUT"/obj/cudaHealpix.o "$OUT"/obj/cudaSphtransf.o \
+    "$OUT"/obj/refdev_harness.o
+echo "build_ref.sh: built $OUT/libpisco_ref.so and $OUT/libpisco_refdev.so"

@@ -1,0 +1,334 @@
+"""Python mirror of the reference API for the convolution path.
+
+Same class names, argument meaning and error behaviour as the reference C++
+classes, so a caller of ``Scan``/``Sky``/``PolBeam``/``Convolver``/
+``GPUConvolver`` finds the same interface:
+
+* ``Scan(nsamples, ra, dec, pa)``        -- src/Scan/scan.hpp:13-26
+* ``Sky(nside, I, Q, U, V)``             -- src/Sky/sky.hpp:15-32
+* ``PolBeam(nside, nPixels, epsilon, enabledDets)`` with ``beam_from_fields``,
+  ``build``, ``make_unpol_gaussian_elliptical_beams`` -- src/Polbeam/polbeam.hpp:26-84
+* ``Convolver(scan, sky, beam).exec_convolution(polFlag, data_a, data_b)``
+  -- src/Convolver/convolver.hpp:18-20 (runs on the GPU here)
+* ``GPUConvolver(RunConfig)`` with ``configure_execution``, ``update_sky``,
+  ``update_beam``, ``update_scan``, ``exec_convolution`` -- src/GpuConvolver/gpuconvolver.hpp:21-34
+
+Every computation goes through libpisco_gb300.so; there is no CPU path.
+Differences from the reference, on purpose: every sample is computed (the
+reference drops ``nsamples % ptgPerConv`` tail samples,
+gpuconvolver.cu:386); errors raise exceptions instead of ``exit(-1)``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (FLOAT32, FLOAT64, FORMS, PiscoError, PiscoInvalidArgument, RunConfig,
+                   check, load, ptr_array)
+
+__all__ = ["Scan", "Sky", "PolBeam", "Convolver", "GPUConvolver", "RunConfig", "PiscoError",
+           "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix"]
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _dtype_code(a: np.ndarray) -> int:
+    if a.dtype == np.float32:
+        return FLOAT32
+    if a.dtype == np.float64:
+        return FLOAT64
+    raise PiscoInvalidArgument(1, "arrays must be float32 or float64, got %s" % a.dtype)
+
+
+# ------------------------------------------------------------------ HEALPix
+def pix2ang(nside: int, pix):
+    L = load()
+    p = np.ascontiguousarray(pix, dtype=np.int64)
+    th = np.empty(p.shape, np.float64)
+    ph = np.empty(p.shape, np.float64)
+    check(L.pisco_hpx_pix2ang(nside, p.size, _ptr(p), _ptr(th), _ptr(ph)), None, "pix2ang")
+    return th, ph
+
+
+def ang2pix(nside: int, theta, phi):
+    L = load()
+    th = np.ascontiguousarray(theta, dtype=np.float64)
+    ph = np.ascontiguousarray(phi, dtype=np.float64)
+    out = np.empty(th.shape, np.int64)
+    check(L.pisco_hpx_ang2pix(nside, th.size, _ptr(th), _ptr(ph), _ptr(out)), None, "ang2pix")
+    return out
+
+
+def beam_npix_for_radius(nside: int, radius_rad: float) -> int:
+    n = load().pisco_beam_npix_for_radius(nside, float(radius_rad))
+    if n < 0:
+        raise PiscoInvalidArgument(1, "bad nside or radius")
+    return int(n)
+
+
+# ------------------------------------------------------------------ API objects
+class Scan:
+    """Non-owning pointing view: ra, dec, pa arrays of length nsamples (radians)."""
+
+    def __init__(self, nsamples: int, ra, dec, pa):
+        self.nsamp = int(nsamples)
+        dt = np.float64 if np.asarray(ra).dtype == np.float64 else np.float32
+        self.ra = np.ascontiguousarray(ra, dtype=dt)
+        self.dec = np.ascontiguousarray(dec, dtype=dt)
+        self.pa = np.ascontiguousarray(pa, dtype=dt)
+        if min(self.ra.size, self.dec.size, self.pa.size) < self.nsamp:
+            raise PiscoInvalidArgument(1, "pointing arrays shorter than nsamples")
+
+    def get_nsamples(self) -> int:
+        return self.nsamp
+
+    def get_ra_ptr(self):
+        return self.ra
+
+    def get_dec_ptr(self):
+        return self.dec
+
+    def get_pa_ptr(self):
+        return self.pa
+
+
+class Sky:
+    """Non-owning view of I, Q, U, V HEALPix RING maps."""
+
+    def __init__(self, nside: int, I, Q, U, V=None):
+        self.nside = int(nside)
+        self.nPixels = 12 * self.nside * self.nside
+        dt = np.float64 if np.asarray(I).dtype == np.float64 else np.float32
+        self.sI = np.ascontiguousarray(I, dtype=dt)
+        self.sQ = np.ascontiguousarray(Q, dtype=dt)
+        self.sU = np.ascontiguousarray(U, dtype=dt)
+        self.sV = None if V is None else np.ascontiguousarray(V, dtype=dt)
+        for m in (self.sI, self.sQ, self.sU) + ((self.sV,) if self.sV is not None else ()):
+            if m.size != self.nPixels:
+                raise PiscoInvalidArgument(1, "map size does not match 12 nside^2")
+
+    def get_nside(self) -> int:
+        return self.nside
+
+    def size(self) -> int:
+        return self.nPixels
+
+
+class PolBeam:
+    """Polarized beam of a detector pair as partial RING maps around the pole.
+
+    nPixels pixels per map; rhoMax = pix2ang(nPixels).theta.  Construction
+    steps run in libpisco_gb300 (host code) with the reference's arithmetic.
+    """
+
+    def __init__(self, nside: int, nPixels: int, epsilon: float, enabledDets: str):
+        L = load()
+        if enabledDets not in ("a", "b", "p"):
+            raise PiscoInvalidArgument(1, "enabledDets must be 'a', 'b' or 'p'")
+        self.nside = int(nside)
+        self.nPixels = int(nPixels)
+        self.epsilon = float(epsilon)
+        self.enabledDets = enabledDets
+        self.rhoMax = L.pisco_beam_rho_max(self.nside, self.nPixels)
+        if self.rhoMax < 0:
+            raise PiscoInvalidArgument(1, "nPixels outside the beam grid")
+        z = lambda: np.zeros(self.nPixels, np.float32)  # noqa: E731
+        self.Ia, self.Qa, self.Ua, self.Va = z(), z(), z(), z()
+        self.Ib, self.Qb, self.Ub, self.Vb = z(), z(), z(), z()
+        self.aBeams = [z() for _ in range(4)]
+        self.bBeams = [z() for _ in range(4)]
+
+    def get_nside(self) -> int:
+        return self.nside
+
+    def size(self) -> int:
+        return self.nPixels
+
+    def get_rho_max(self) -> float:
+        return self.rhoMax
+
+    def beam_from_fields(self, polFlag: str, magEco, phsEco, magEcx, phsEcx) -> None:
+        L = load()
+        f = [np.ascontiguousarray(x, dtype=np.float64) for x in (magEco, phsEco, magEcx, phsEcx)]
+        if polFlag == "a":
+            out = (self.Ia, self.Qa, self.Ua, self.Va)
+        elif polFlag == "b":
+            out = (self.Ib, self.Qb, self.Ub, self.Vb)
+        else:
+            raise PiscoInvalidArgument(1, "polFlag must be 'a' or 'b'")
+        check(L.pisco_beam_from_fields(self.nPixels, *[_ptr(x) for x in f],
+                                       *[_ptr(x) for x in out]), None, "beam_from_fields")
+
+    def build(self, nsideSky: int) -> None:
+        L = load()
+        ta = ptr_array([x.ctypes.data for x in (self.Ia, self.Qa, self.Ua, self.Va)])
+        tb = ptr_array([x.ctypes.data for x in (self.Ib, self.Qb, self.Ub, self.Vb)])
+        oa = ptr_array([x.ctypes.data for x in self.aBeams])
+        ob = ptr_array([x.ctypes.data for x in self.bBeams])
+        check(L.pisco_beam_build(self.nside, self.nPixels, self.epsilon,
+                                 self.enabledDets.encode(), int(nsideSky), ta, tb, oa, ob),
+              None, "build")
+
+    def make_unpol_gaussian_elliptical_beams(self, fwhmx: float, fwhmy: float, phi0: float) -> None:
+        L = load()
+        f = [np.empty(self.nPixels, np.float64) for _ in range(4)]
+        check(L.pisco_beam_gaussian_fields(self.nside, self.nPixels, float(fwhmx), float(fwhmy),
+                                           float(phi0), *[_ptr(x) for x in f]), None,
+              "make_unpol_gaussian_elliptical_beams")
+        if self.enabledDets in ("a", "p"):
+            self.beam_from_fields("a", *f)
+        if self.enabledDets in ("b", "p"):
+            self.beam_from_fields("b", *f)
+
+    def planes(self):
+        """(a, b) as 4 x nPixels float32 arrays."""
+        return np.stack(self.aBeams), np.stack(self.bBeams)
+
+
+# ------------------------------------------------------------------ convolvers
+class GPUConvolver:
+    """Drop-in for the reference GPUConvolver on one GB300.
+
+    ``form``: "plain" (the reference chain), "tuned" (FP32 per-pair geometry
+    with FP64 re-evaluation near pixel edges) or "fp64".
+    """
+
+    def __init__(self, cfg: RunConfig | None = None, form: str = "plain"):
+        self.cfg = cfg if cfg is not None else RunConfig()
+        self.form = form
+        if form not in FORMS:
+            raise PiscoInvalidArgument(1, "form must be one of %s" % sorted(FORMS))
+        self._ctx = None
+        self._n = 0
+
+    # the reference allocates in configure_execution (gpuconvolver.cu:72-87)
+    def configure_execution(self) -> None:
+        L = load()
+        h = ctypes.c_void_p()
+        st = L.pisco_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if st != 0:
+            msg = L.pisco_last_error(None).decode()
+            if st in (_lib.PISCO_ERR_INVALID_CONFIG, _lib.PISCO_ERR_INVALID_ARGUMENT):
+                raise PiscoInvalidArgument(st, msg)
+            raise PiscoError(st, msg)
+        self._ctx = h
+
+    @property
+    def ctx(self):
+        if self._ctx is None:
+            self.configure_execution()
+        return self._ctx
+
+    def __del__(self):
+        if getattr(self, "_ctx", None) is not None:
+            try:
+                load().pisco_destroy(self._ctx)
+            except Exception:  # noqa: BLE001 -- interpreter shutdown
+                pass
+            self._ctx = None
+
+    def close(self) -> None:
+        self.__del__()
+
+    def update_sky(self, sky: Sky) -> None:
+        V = sky.sV
+        check(load().pisco_set_sky(self.ctx, sky.nside, _ptr(sky.sI), _ptr(sky.sQ), _ptr(sky.sU),
+                                   _ptr(V), _dtype_code(sky.sI)), self.ctx, "update_sky")
+
+    def update_beam(self, beam: PolBeam) -> None:
+        self.set_beam_planes(beam.nside, beam.nPixels, beam.aBeams, beam.bBeams)
+
+    def set_beam_planes(self, nside: int, npix: int, a, b) -> None:
+        a = [np.ascontiguousarray(x) for x in a]
+        b = [np.ascontiguousarray(x) for x in b]
+        dt = _dtype_code(a[0])
+        a = [np.ascontiguousarray(x, dtype=a[0].dtype) for x in a]
+        b = [np.ascontiguousarray(x, dtype=a[0].dtype) for x in b]
+        self._keep = (a, b)
+        check(load().pisco_set_beam(self.ctx, int(nside), int(npix),
+                                    ptr_array([x.ctypes.data for x in a]),
+                                    ptr_array([x.ctypes.data for x in b]), dt),
+              self.ctx, "update_beam")
+
+    def update_scan(self, scan: Scan) -> None:
+        self._n = scan.nsamp
+        check(load().pisco_set_scan(self.ctx, scan.nsamp, _ptr(scan.ra), _ptr(scan.dec),
+                                    _ptr(scan.pa), _dtype_code(scan.ra)), self.ctx, "update_scan")
+
+    def set_interp(self, bilinear: bool) -> None:
+        check(load().pisco_set_interp(self.ctx, 1 if bilinear else 0), self.ctx, "set_interp")
+
+    def exec_convolution(self, data_a: np.ndarray, data_b: np.ndarray, polFlag: str = "p",
+                         form: str | None = None) -> None:
+        """Fill data_a/data_b (float32 or float64 arrays of nsamples) in place."""
+        f = FORMS[form or self.form]
+        ref = data_a if data_a is not None else data_b
+        dt = _dtype_code(ref)
+        for d in (data_a, data_b):
+            if d is not None and (not d.flags["C_CONTIGUOUS"] or d.size < self._n or
+                                  _dtype_code(d) != dt):
+                raise PiscoInvalidArgument(1, "output arrays must be contiguous, of one dtype "
+                                              "and hold nsamples values")
+        check(load().pisco_forward(self.ctx, polFlag.encode(), _ptr(data_a), _ptr(data_b), dt, f),
+              self.ctx, "exec_convolution")
+
+    # ---- resident-input entry points (torch / benchmarks)
+    def forward_device(self, d_a: int, d_b: int, out_f64: bool = False, begin: int = 0,
+                       n: int | None = None, stream: int = 0, form: str | None = None) -> None:
+        n = self._n - begin if n is None else n
+        check(load().pisco_forward_device(self.ctx, FORMS[form or self.form], begin, n, d_a or None,
+                                          d_b or None, FLOAT64 if out_f64 else FLOAT32,
+                                          stream or None), self.ctx, "forward_device")
+
+    def sync(self) -> None:
+        check(load().pisco_sync(self.ctx), self.ctx, "sync")
+
+    def set_scan_device(self, n: int, d_ra: int, d_dec: int, d_pa: int, stream: int = 0) -> None:
+        self._n = int(n)
+        check(load().pisco_set_scan_device(self.ctx, int(n), d_ra, d_dec, d_pa, stream or None),
+              self.ctx, "set_scan_device")
+
+    def set_sky_device(self, nside: int, d_iquv: int, f64: bool, stream: int = 0) -> None:
+        check(load().pisco_set_sky_device(self.ctx, int(nside), d_iquv, FLOAT64 if f64 else FLOAT32,
+                                          stream or None), self.ctx, "set_sky_device")
+
+    def count_pairs(self) -> int:
+        v = ctypes.c_longlong()
+        check(load().pisco_count_pairs(self.ctx, ctypes.byref(v)), self.ctx, "count_pairs")
+        return int(v.value)
+
+    def last_fallbacks(self) -> int:
+        v = ctypes.c_longlong()
+        check(load().pisco_last_fallbacks(self.ctx, ctypes.byref(v)), self.ctx, "last_fallbacks")
+        return int(v.value)
+
+
+class Convolver:
+    """``Convolver(scan, sky, beam).exec_convolution(polFlag, data_a, data_b)``.
+
+    Same call as the reference CPU Convolver (convolver.cpp:22-72); the work
+    runs on the GPU through a private GPUConvolver.  ``polFlag`` other than
+    'a', 'b', 'p' raises ``PiscoInvalidArgument`` (std::invalid_argument in
+    the reference).
+    """
+
+    def __init__(self, scan: Scan, sky: Sky, beam: PolBeam, form: str = "plain"):
+        self.scan, self.sky, self.beam = scan, sky, beam
+        self.form = form
+
+    def exec_convolution(self, polFlag: str, data_a: np.ndarray, data_b: np.ndarray) -> None:
+        if polFlag not in ("a", "b", "p"):
+            raise PiscoInvalidArgument(1, "valid polFlags are 'a', 'b' and 'p'")
+        g = GPUConvolver(RunConfig(), form=self.form)
+        try:
+            g.update_sky(self.sky)
+            g.update_beam(self.beam)
+            g.update_scan(self.scan)
+            g.exec_convolution(data_a if polFlag in "ap" else None,
+                               data_b if polFlag in "bp" else None, polFlag=polFlag)
+        finally:
+            g.close()

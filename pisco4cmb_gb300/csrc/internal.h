@@ -1,0 +1,77 @@
+// internal.h -- device data layout and kernel launchers of libpisco_gb300.
+//
+// HBM layout (all RING-ordered, resident for the life of a context):
+//   sky32  float4[npix]         I,Q,U,V interleaved, one 16-byte load per pixel
+//   sky64  D4[npix]             FP64 copy for the FP64 form (32 bytes/pixel)
+//   beam32 F8[npixB]            a.IQUV | b.IQUV: both detectors of one beam
+//                               pixel in one 32-byte sector
+//   beam64 D8[npixB]            FP64 copy (64 bytes/pixel)
+//   ra/dec/pa double[n]         FP64 pointing (structure of arrays)
+//   out    float|double[n]      TOD a and b
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pisco {
+
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+struct alignas(32) F8 {
+    float4 a, b;
+};
+struct alignas(64) D8 {
+    D4 a, b;
+};
+
+// Device-side check codes written to the context's error word (first one
+// wins).  Kernels never trap: they record the code, skip the access and
+// finish.
+enum DevCheck : unsigned int {
+    kCheckOk = 0,
+    kCheckSkyIndex = 1,
+    kCheckBeamIndex = 2,
+    kCheckFallbackOverflow = 3,
+    kCheckQueue = 4,
+    kCheckAdjointIndex = 5,
+};
+
+struct FwdArgs {
+    int nside_sky;
+    const float4* sky32;
+    const D4* sky64;
+    int nside_beam;
+    int npix_beam;
+    const F8* beam32;
+    const D8* beam64;
+    double rho_max;
+    long long begin, n;
+    const double* ra;
+    const double* dec;
+    const double* pa;
+    void* out_a;  // may be null
+    void* out_b;  // may be null
+    int out_f64;
+    int interp;  // 0 nearest, 1 bilinear
+    unsigned int* err;
+    unsigned long long* fallbacks;  // tuned form: pairs re-evaluated in FP64
+};
+
+// PLAIN (f64 = false) and FP64 (f64 = true) forms.
+cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaStream_t st);
+// TUNED form; returns cudaErrorNotSupported when the beam does not fit the
+// north polar cap of its grid (the tuned geometry's domain).
+cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st);
+bool tuned_supported(int nside_beam, int npix_beam, double rho_max);
+// Per-sample disc sizes (pairs) for the roofline byte model.
+cudaError_t launch_count_pairs(int nside_sky, double rho_max, long long n, const double* ra,
+                               const double* dec, unsigned long long* total, int sm_count,
+                               cudaStream_t st);
+// float -> double widening and scan conversion helpers.
+cudaError_t launch_widen_sky(const float4* in, D4* out, long long npix, cudaStream_t st);
+cudaError_t launch_widen_beam(const F8* in, D8* out, long long npix, cudaStream_t st);
+cudaError_t launch_f32_to_f64(const float* in, double* out, long long n, cudaStream_t st);
+cudaError_t launch_narrow_sky(const D4* in, float4* out, long long npix, cudaStream_t st);
+
+}  // namespace pisco

@@ -1,0 +1,174 @@
+"""Parity of the CUDA forward forms, called through the C ABI (GPU).
+
+Tolerances (relative to the TOD rms):
+* PLAIN vs the reference Convolver (golden fixtures, float API): max 1e-6 --
+  same float per-pair products, only rounding/contraction order differs.
+* FP64 vs the oracle's all-double form on the same inputs: max 1e-12.
+* TUNED vs FP64 on the same float inputs: rms 1e-6 (the target), and every
+  beam-pixel decision identical (tested through the TOD at 1e-6 max).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_max, rel_rms
+
+pytestmark = pytest.mark.gpu
+
+
+def make_conv(g, form="plain", sky64=False, beam64=False, ptg64=False, cfg=None):
+    from pisco4cmb_gb300 import GPUConvolver, RunConfig, Scan, Sky
+
+    c = GPUConvolver(cfg or RunConfig(), form=form)
+    sky = g["sky"] if sky64 else g["sky"].astype(np.float32)
+    c.update_sky(Sky(int(g["nside_sky"]), sky[0], sky[1], sky[2], None))
+    a = [g["beam_a"][k].astype(np.float64 if beam64 else np.float32) for k in range(4)]
+    b = [g["beam_b"][k].astype(np.float64 if beam64 else np.float32) for k in range(4)]
+    c.set_beam_planes(int(g["nside_beam"]), int(g["npix_beam"]), a, b)
+    dt = np.float64 if ptg64 else np.float32
+    n = g["ra"].size
+    c.update_scan(Scan(n, g["ra"].astype(dt), g["dec"].astype(dt), g["pa"].astype(dt)))
+    return c
+
+
+def run(c, n, dtype=np.float32, form=None, polflag="p"):
+    a = np.full(n, np.nan, dtype)
+    b = np.full(n, np.nan, dtype)
+    c.exec_convolution(a, b, polFlag=polflag, form=form)
+    return a, b
+
+
+@pytest.mark.parametrize("case", ["golden_c1", "golden_ellip"])
+def test_plain_matches_reference_convolver(gpu, case, request):
+    g = request.getfixturevalue(case)
+    c = make_conv(g)
+    a, b = run(c, g["ra"].size)
+    assert rel_max(a, g["tod_a"]) < 1e-6
+    assert rel_max(b, g["tod_b"]) < 1e-6
+
+
+@pytest.mark.parametrize("case", ["golden_c1", "golden_ellip"])
+def test_fp64_matches_double_oracle(gpu, oracle_mod, case, request):
+    g = request.getfixturevalue(case)
+    c = make_conv(g, form="fp64", sky64=True, beam64=True, ptg64=True)
+    a, b = run(c, g["ra"].size, np.float64)
+    oa, ob = oracle_mod.convolve_f64(g["ra"].astype(np.float64), g["dec"].astype(np.float64),
+                                     g["pa"].astype(np.float64), int(g["nside_sky"]), g["sky"],
+                                     int(g["nside_beam"]), g["beam_a"].astype(np.float64),
+                                     g["beam_b"].astype(np.float64))
+    assert rel_max(a, oa) < 1e-12
+    assert rel_max(b, ob) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["golden_c1", "golden_ellip"])
+def test_tuned_matches_fp64(gpu, case, request):
+    g = request.getfixturevalue(case)
+    ref = make_conv(g, form="fp64", ptg64=True)
+    ra, rb = run(ref, g["ra"].size, np.float64)
+    c = make_conv(g, form="tuned", ptg64=True)
+    a, b = run(c, g["ra"].size, np.float64)
+    assert rel_rms(a, ra) < 1e-6 and rel_rms(b, rb) < 1e-6
+    assert rel_max(a, ra) < 1e-6 and rel_max(b, rb) < 1e-6
+
+
+def test_bilinear_matches_oracle(gpu, oracle_mod, golden_ellip):
+    g = golden_ellip
+    c = make_conv(g, form="fp64", sky64=True, beam64=True, ptg64=True)
+    c.set_interp(True)
+    a, b = run(c, g["ra"].size, np.float64)
+    oa, ob = oracle_mod.convolve_f64(g["ra"].astype(np.float64), g["dec"].astype(np.float64),
+                                     g["pa"].astype(np.float64), int(g["nside_sky"]), g["sky"],
+                                     int(g["nside_beam"]), g["beam_a"].astype(np.float64),
+                                     g["beam_b"].astype(np.float64), interp=1)
+    assert rel_max(a, oa) < 1e-12 and rel_max(b, ob) < 1e-12
+    c2 = make_conv(g, form="plain")
+    c2.set_interp(True)
+    pa_, pb_ = run(c2, g["ra"].size)
+    fa, fb = oracle_mod.convolve_f32(g["ra"], g["dec"], g["pa"], int(g["nside_sky"]),
+                                     g["sky"].astype(np.float32), int(g["nside_beam"]),
+                                     g["beam_a"], g["beam_b"], interp=1)
+    assert rel_max(pa_, fa) < 1e-6 and rel_max(pb_, fb) < 1e-6
+
+
+def test_polflag_tail_and_determinism(gpu, golden_c1):
+    from pisco4cmb_gb300 import PiscoInvalidArgument, RunConfig
+
+    g = golden_c1
+    n = g["ra"].size
+    # ptgPerConv that does not divide n: the reference drops the tail; here
+    # every sample is computed
+    c = make_conv(g, cfg=RunConfig(ptgPerConv=7777))
+    a1, b1 = run(c, n)
+    assert np.all(np.isfinite(a1)) and np.all(np.isfinite(b1))
+    a2, b2 = run(c, n)
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)  # deterministic
+    a = np.full(n, np.nan, np.float32)
+    c.exec_convolution(a, None, polFlag="a")
+    assert np.array_equal(a, a1)
+    b = np.full(n, np.nan, np.float32)
+    c.exec_convolution(None, b, polFlag="b")
+    assert np.array_equal(b, b1)
+    with pytest.raises(PiscoInvalidArgument):
+        c.exec_convolution(a, b, polFlag="x")
+
+
+def test_convolver_dropin_api(gpu, golden_c1):
+    from pisco4cmb_gb300 import Convolver, PolBeam, PiscoInvalidArgument, Scan, Sky
+
+    g = golden_c1
+    sky = g["sky"].astype(np.float32)
+    beam = PolBeam(int(g["nside_beam"]), int(g["npix_beam"]), 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(2.0, 2.0, 0.0)
+    beam.build(int(g["nside_sky"]))
+    n = g["ra"].size
+    conv = Convolver(Scan(n, g["ra"], g["dec"], g["pa"]),
+                     Sky(int(g["nside_sky"]), sky[0], sky[1], sky[2], np.zeros_like(sky[0])), beam)
+    a = np.zeros(n, np.float32)
+    b = np.zeros(n, np.float32)
+    conv.exec_convolution("p", a, b)
+    assert rel_max(a, g["tod_a"]) < 1e-6 and rel_max(b, g["tod_b"]) < 1e-6
+    with pytest.raises(PiscoInvalidArgument):
+        conv.exec_convolution("q", a, b)
+
+
+def test_pair_count_and_empty_scan(gpu, oracle_mod, golden_ellip):
+    from pisco4cmb_gb300 import Scan
+
+    g = golden_ellip
+    c = make_conv(g)
+    want = sum(oracle_mod.query_disc(int(g["nside_sky"]), np.pi / 2 - float(np.float64(d)),
+                                     float(np.float64(r)), float(g["rho_max"])).size
+               for r, d in zip(g["ra"], g["dec"]))
+    assert c.count_pairs() == want
+    c.update_scan(Scan(0, np.zeros(0, np.float32), np.zeros(0, np.float32), np.zeros(0, np.float32)))
+    a = np.zeros(0, np.float32)
+    c.exec_convolution(a, a.copy())
+    c.sync()
+
+
+def test_edge_pointings(gpu, oracle_mod):
+    """Poles, ra wrap, negative ra, tiny and whole-ring discs, nside 1 sky."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky
+
+    rng = np.random.default_rng(9)
+    for nss, nsb, rdeg in ((1, 64, 10.0), (8, 128, 20.0), (64, 512, 2.0)):
+        npix = 12 * nss * nss
+        sky = rng.normal(size=(3, npix))
+        beam = PolBeam(nsb, oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(rdeg)), 0.0, "p")
+        beam.make_unpol_gaussian_elliptical_beams(rdeg / 2, rdeg / 3, 10.0)
+        beam.build(nss)
+        ra = np.array([0.0, 2 * np.pi - 1e-9, -0.3, 7.0, 1.0, 2.0, 3.0, 0.5])
+        dec = np.array([np.pi / 2, -np.pi / 2, 0.1, -0.2, np.pi / 2 - 1e-7, -np.pi / 2 + 1e-4,
+                        0.0, 1.0])
+        pa = rng.uniform(-3, 3, ra.size)
+        c = GPUConvolver(form="fp64")
+        c.update_sky(Sky(nss, *sky, None))
+        c.update_beam(beam)
+        c.update_scan(Scan(ra.size, ra, dec, pa))
+        a = np.zeros(ra.size)
+        b = np.zeros(ra.size)
+        c.exec_convolution(a, b)
+        pa_, pb_ = beam.planes()
+        oa, ob = oracle_mod.convolve_f64(ra, dec, pa, nss, sky, nsb, pa_.astype(np.float64),
+                                         pb_.astype(np.float64))
+        np.testing.assert_allclose(a, oa, rtol=0, atol=1e-12 * max(1.0, np.abs(oa).max()))
+        np.testing.assert_allclose(b, ob, rtol=0, atol=1e-12 * max(1.0, np.abs(ob).max()))
