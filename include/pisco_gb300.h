@@ -129,6 +129,11 @@ pisco_status pisco_sync(pisco_ctx* ctx);
  * pairs the TUNED form re-evaluated in FP64. */
 pisco_status pisco_count_pairs(pisco_ctx* ctx, long long* pairs);
 pisco_status pisco_last_fallbacks(pisco_ctx* ctx, long long* fallbacks);
+/* Diagnostic (no reference counterpart): runs the TUNED form on samples
+ * [begin, begin+n) with each FP32 pixel decision also evaluated in FP64 and
+ * returns the worst FP32 error as a fraction of the FP64 re-evaluation
+ * margin (must stay well below 1).  Outputs are discarded. */
+pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* worst_fraction);
 
 /* ---- host HEALPix / PolBeam helpers (for the C++ PolBeam wrapper) ------ */
 /* Healpix_Base::pix2ang / ang2pix, RING (used by polbeam.cpp:130,441). */

@@ -83,6 +83,7 @@ SIGNATURES = [
     ("pisco_sync", _S, [_P]),
     ("pisco_count_pairs", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_last_fallbacks", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double)]),
     ("pisco_hpx_pix2ang", _S, [_I, _L, _P, _P, _P]),
     ("pisco_hpx_ang2pix", _S, [_I, _L, _P, _P, _P]),
     ("pisco_beam_npix_for_radius", _L, [_I, _D]),
@@ -128,7 +129,7 @@ def check(status: int, ctx=None, what: str = "") -> None:
     if status == PISCO_OK:
         return
     L = load()
-    msg = L.pisco_last_error(ctx).decode() if True else ""
+    msg = L.pisco_last_error(ctx).decode()
     text = "%s: %s (%s)" % (what, msg or L.pisco_status_string(status).decode(),
                             L.pisco_status_string(status).decode())
     if status == PISCO_ERR_INVALID_ARGUMENT:

@@ -301,6 +301,14 @@ class GPUConvolver:
         check(load().pisco_count_pairs(self.ctx, ctypes.byref(v)), self.ctx, "count_pairs")
         return int(v.value)
 
+    def tuned_calibrate(self, begin: int = 0, n: int | None = None) -> float:
+        """Worst FP32 decision error of the TUNED form as a fraction of its margin."""
+        n = self._n - begin if n is None else n
+        v = ctypes.c_double()
+        check(load().pisco_tuned_calibrate(self.ctx, begin, n, ctypes.byref(v)), self.ctx,
+              "tuned_calibrate")
+        return float(v.value)
+
     def last_fallbacks(self) -> int:
         v = ctypes.c_longlong()
         check(load().pisco_last_fallbacks(self.ctx, ctypes.byref(v)), self.ctx, "last_fallbacks")

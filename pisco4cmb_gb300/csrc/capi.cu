@@ -584,4 +584,41 @@ pisco_status pisco_last_fallbacks(pisco_ctx* c, long long* fallbacks)
     return PISCO_OK;
 }
 
+pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* worst)
+{
+    if (!c || !worst) return PISCO_ERR_INVALID_ARGUMENT;
+    if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
+    if (begin < 0 || n < 0 || begin + n > c->nsamples)
+        return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sample range outside the scan");
+    if (!tuned_supported(c->nside_beam, (int)c->npix_beam, c->rho_max))
+        return fail(c, PISCO_ERR_UNSUPPORTED, "beam outside the tuned form's domain");
+    pisco_status st = c->activate();
+    if (st != PISCO_OK) return st;
+    float* d = nullptr;
+    CK(cudaMalloc(&d, sizeof(float)), "calib buffer");
+    cudaMemsetAsync(d, 0, sizeof(float), c->stream);
+    FwdArgs a{};
+    a.nside_sky = c->nside_sky;
+    a.sky32 = c->sky32;
+    a.nside_beam = c->nside_beam;
+    a.npix_beam = (int)c->npix_beam;
+    a.beam32 = c->beam32;
+    a.rho_max = c->rho_max;
+    a.begin = begin;
+    a.n = n;
+    a.ra = c->ra;
+    a.dec = c->dec;
+    a.pa = c->pa;
+    a.err = c->d_err;
+    a.fallbacks = c->d_fallbacks;
+    cudaError_t e = launch_tuned_calibrate(a, c->sm_count, c->stream, d);
+    float v = 0.0f;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&v, d, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(c, e, "calibration");
+    *worst = v;
+    return c->check_device();
+}
+
 }  // extern "C"

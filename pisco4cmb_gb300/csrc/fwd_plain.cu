@@ -16,6 +16,8 @@
 // per lane, flattens their pixel ranges with a warp scan and strides the
 // pairs across lanes; the per-lane sums are combined by a fixed shuffle
 // tree, so every output is bit-for-bit reproducible.
+#include <math_constants.h>
+
 #include "hpx.cuh"
 #include "internal.h"
 
@@ -171,6 +173,19 @@ __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
     for (long long i = gw; i < a.n; i += nw) {
         const long long s = a.begin + i;
         const double ra = a.ra[s], dec = a.dec[s], psi = -a.pa[s];
+        if (!(isfinite(ra) && isfinite(dec) && isfinite(psi))) {
+            // non-finite pointing: NaN out (never let it reach the ring loop bounds)
+            if (lane == 0) {
+                if (a.out_f64) {
+                    if (a.out_a) ((double*)a.out_a)[i] = CUDART_NAN;
+                    if (a.out_b) ((double*)a.out_b)[i] = CUDART_NAN;
+                } else {
+                    if (a.out_a) ((float*)a.out_a)[i] = CUDART_NAN_F;
+                    if (a.out_b) ((float*)a.out_b)[i] = CUDART_NAN_F;
+                }
+            }
+            continue;
+        }
         const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, dec), ra, a.rho_max);
         double acc_a = 0.0, acc_b = 0.0;
         for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
@@ -228,6 +243,7 @@ __global__ void __launch_bounds__(256) count_kernel(int nside_sky, double rho_ma
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long mine = 0;
     for (long long s = gw; s < n; s += nw) {
+        if (!(isfinite(ra[s]) && isfinite(dec[s]))) continue;
         const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, dec[s]), ra[s], rho_max);
         for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
             const long long ring = r0 + lane;

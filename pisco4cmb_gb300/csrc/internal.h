@@ -64,6 +64,9 @@ cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaS
 // north polar cap of its grid (the tuned geometry's domain).
 cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st);
 bool tuned_supported(int nside_beam, int npix_beam, double rho_max);
+// Same kernel with every FP32 decision also evaluated in FP64: writes the
+// worst |FP32 - FP64| / margin seen over the non-fallback pairs to *calib.
+cudaError_t launch_tuned_calibrate(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib);
 // Per-sample disc sizes (pairs) for the roofline byte model.
 cudaError_t launch_count_pairs(int nside_sky, double rho_max, long long n, const double* ra,
                                const double* dec, unsigned long long* total, int sm_count,

@@ -69,9 +69,16 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
     cl = np.zeros(M)
     cl[lmin:] = ell[lmin:] ** -2.0
     F = torch.zeros((M, R), dtype=torch.complex128, device=dev)
+    # Values are carried as v * BIG**E with a per-(m, ring) integer exponent
+    # E: lambda_mm ~ sin(theta)^m leaves the double range for large m, and
+    # the recurrence started from an underflowed value diverges.  Only rows
+    # back at scale E == 0 contribute (E < 0 rows are below 1e-100).
+    BIG = 1e100
     lam_mm = torch.full((R,), math.sqrt(1.0 / (4 * math.pi)), dtype=torch.float64, device=dev)
+    e_mm = torch.zeros(R, dtype=torch.int32, device=dev)
     lm1 = torch.zeros((M, R), dtype=torch.float64, device=dev)  # lambda_{l-1, m}
     lm2 = torch.zeros((M, R), dtype=torch.float64, device=dev)  # lambda_{l-2, m}
+    E = torch.zeros((M, R), dtype=torch.int32, device=dev)
     for l in range(0, M):
         cur = torch.zeros((M, R), dtype=torch.float64, device=dev)
         if l >= 1:
@@ -82,7 +89,17 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
                 cur[: l - 1] = a[:, None] * (zt[None, :] * lm1[: l - 1] - b[:, None] * lm2[: l - 1])
             cur[l - 1] = math.sqrt(2.0 * l + 1.0) * zt * lm1[l - 1]
             lam_mm = -math.sqrt((2.0 * l + 1.0) / (2.0 * l)) * st * lam_mm
+            small = (lam_mm.abs() < 1.0 / BIG) & (lam_mm != 0)
+            lam_mm = torch.where(small, lam_mm * BIG, lam_mm)
+            e_mm = e_mm - small.to(torch.int32)
         cur[l] = lam_mm
+        E[l] = e_mm
+        # rescale rows that grew past BIG (both retained terms share E)
+        big = cur[: l + 1].abs() > BIG
+        if bool(big.any()):
+            cur[: l + 1] = torch.where(big, cur[: l + 1] / BIG, cur[: l + 1])
+            lm1[: l + 1] = torch.where(big, lm1[: l + 1] / BIG, lm1[: l + 1])
+            E[: l + 1] += big.to(torch.int32)
         if cl[l] > 0:
             sd = math.sqrt(cl[l])
             re = rng.standard_normal(l + 1) * sd
@@ -91,7 +108,8 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
             im[1:] *= math.sqrt(0.5)
             im[0] = 0.0
             alm = torch.tensor(re + 1j * im, dtype=torch.complex128, device=dev)
-            F[: l + 1] += alm[:, None] * cur[: l + 1]
+            live = torch.where(E[: l + 1] == 0, cur[: l + 1], torch.zeros_like(cur[: l + 1]))
+            F[: l + 1] += alm[:, None] * live
         lm2, lm1 = lm1, cur
     # per ring: T(phi_j) = F_0 + 2 Re sum_{m>0} F_m e^{i m phi_j}
     out = np.empty(int(start[-1] + n_in[-1]), np.float64)
