@@ -135,6 +135,74 @@ pisco_status pisco_last_fallbacks(pisco_ctx* ctx, long long* fallbacks);
  * margin (must stay well below 1).  Outputs are discarded. */
 pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* worst_fraction);
 
+/* ---- batched multi-detector forward ------------------------------------ */
+/* One detector pair of a batched forward.  Device pointers: FP64 pointing
+ * of nsamples samples and the two TOD outputs (out_dtype; either may be
+ * NULL).  The reference handles one pair per GPUConvolver
+ * (gpuconvolver.hpp:17-82); a focal plane is a loop over such objects. */
+typedef struct pisco_det_desc {
+    int beam_slot; /* beam set with pisco_set_beam_slot */
+    int reserved;
+    long long nsamples;
+    const double* ra;
+    const double* dec;
+    const double* pa;
+    void* tod_a;
+    void* tod_b;
+} pisco_det_desc;
+
+/* Beam of one detector pair (PolBeam::aBeams / bBeams planes), kept in slot
+ * `slot` (0 <= slot < 1024) for batched launches; same arguments as
+ * pisco_set_beam. */
+pisco_status pisco_set_beam_slot(pisco_ctx* ctx, int slot, int nside, long npix,
+                                 const void* const a[4], const void* const b[4],
+                                 pisco_dtype dtype);
+/* All pairs in one persistent TUNED launch over a (detector, sample-chunk)
+ * work queue, longest chunks first.  chunk = samples per queue item (0 =
+ * the last autotuned value, else 256).  The launch is captured in a CUDA
+ * graph and replayed while the same descriptors and chunk are resubmitted.
+ * Asynchronous on `stream` (NULL = context stream); pisco_sync() reports
+ * device-side check failures.  Every beam must fit the TUNED form's domain
+ * (PISCO_ERR_UNSUPPORTED otherwise). */
+pisco_status pisco_forward_batched(pisco_ctx* ctx, const pisco_det_desc* dets, int ndet,
+                                   pisco_dtype out_dtype, int chunk, void* stream);
+/* Autotuner (no reference counterpart): times the batched launch for chunk
+ * sizes 32..8192 on these descriptors, keeps the fastest in the context and,
+ * if cache_path is not NULL, in a JSON object keyed by device, sky nside,
+ * beam set and form (read first: a cached key is reused without timing).
+ * Returns the chosen chunk and its time in ms. */
+pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, int ndet,
+                                    pisco_dtype out_dtype, const char* cache_path,
+                                    int* chunk_out, double* ms_out);
+
+/* ---- adjoint (no reference counterpart: PISCO has no gradient) --------- */
+/* ATOMIC: float atomics, fast, last bits vary run to run.
+ * DETERMINISTIC: 64-bit fixed-point atomics with a scale from a rigorous
+ * bound on every total; bit-identical results whatever the order. */
+typedef enum pisco_adjoint_mode {
+    PISCO_ADJ_ATOMIC = 0,
+    PISCO_ADJ_DETERMINISTIC = 1
+} pisco_adjoint_mode;
+
+/* Beam from a device buffer of npix x 8 interleaved values (a.I,Q,U,V,
+ * b.I,Q,U,V), e.g. a beam built by differentiable code on the GPU. */
+pisco_status pisco_set_beam_device(pisco_ctx* ctx, int nside, long npix, const void* d_ab,
+                                   pisco_dtype dtype, void* stream);
+/* Transpose of the TUNED forward over samples [begin, begin+n) of the
+ * current scan: d_ga, d_gb = dL/dTOD a, b (n values of g_dtype, device).
+ * Writes (overwrites) d_gsky = dL/dsky as npix x 4 (I,Q,U,V interleaved) and
+ * d_gbeam = dL/dbeam as npixB x 8 (a.IQUV, b.IQUV), either may be NULL, in
+ * out_dtype.  The pair set and beam pixels are exactly the forward's. */
+pisco_status pisco_adjoint_device(pisco_ctx* ctx, long begin, long n, const void* d_ga,
+                                  const void* d_gb, pisco_dtype g_dtype, void* d_gsky,
+                                  void* d_gbeam, pisco_dtype out_dtype, pisco_adjoint_mode mode,
+                                  void* stream);
+/* Host arrays: g_a, g_b (nsamples each) in; sky gradient planes out (any of
+ * gI, gQ, gU, gV may be NULL). */
+pisco_status pisco_adjoint(pisco_ctx* ctx, const void* g_a, const void* g_b, pisco_dtype g_dtype,
+                           void* gI, void* gQ, void* gU, void* gV, pisco_dtype out_dtype,
+                           pisco_adjoint_mode mode);
+
 /* ---- host HEALPix / PolBeam helpers (for the C++ PolBeam wrapper) ------ */
 /* Healpix_Base::pix2ang / ang2pix, RING (used by polbeam.cpp:130,441). */
 pisco_status pisco_hpx_pix2ang(int nside, long n, const long* pix, double* theta, double* phi);

@@ -59,6 +59,15 @@ class RunConfig(ctypes.Structure):
                          blockSizeY, ptgPerConv, pixelsPerDisc)
 
 
+class DetDesc(ctypes.Structure):
+    """pisco_det_desc: one detector pair of a batched forward (device pointers)."""
+
+    _fields_ = [("beam_slot", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("nsamples", ctypes.c_longlong), ("ra", ctypes.c_void_p),
+                ("dec", ctypes.c_void_p), ("pa", ctypes.c_void_p),
+                ("tod_a", ctypes.c_void_p), ("tod_b", ctypes.c_void_p)]
+
+
 # every symbol the header declares: (name, restype, argtypes)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -84,6 +93,13 @@ SIGNATURES = [
     ("pisco_count_pairs", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_last_fallbacks", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double)]),
+    ("pisco_set_beam_slot", _S, [_P, _I, _I, _L, _PP, _PP, _I]),
+    ("pisco_forward_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, _I, _P]),
+    ("pisco_autotune_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, ctypes.c_char_p,
+                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    ("pisco_set_beam_device", _S, [_P, _I, _L, _P, _I, _P]),
+    ("pisco_adjoint_device", _S, [_P, _L, _L, _P, _P, _I, _P, _P, _I, _I, _P]),
+    ("pisco_adjoint", _S, [_P, _P, _P, _I, _P, _P, _P, _P, _I, _I]),
     ("pisco_hpx_pix2ang", _S, [_I, _L, _P, _P, _P]),
     ("pisco_hpx_ang2pix", _S, [_I, _L, _P, _P, _P]),
     ("pisco_beam_npix_for_radius", _L, [_I, _D]),

@@ -235,6 +235,7 @@ class GPUConvolver:
         self.__del__()
 
     def update_sky(self, sky: Sky) -> None:
+        self._npix_sky = sky.nPixels
         V = sky.sV
         check(load().pisco_set_sky(self.ctx, sky.nside, _ptr(sky.sI), _ptr(sky.sQ), _ptr(sky.sU),
                                    _ptr(V), _dtype_code(sky.sI)), self.ctx, "update_sky")
@@ -293,6 +294,7 @@ class GPUConvolver:
               self.ctx, "set_scan_device")
 
     def set_sky_device(self, nside: int, d_iquv: int, f64: bool, stream: int = 0) -> None:
+        self._npix_sky = 12 * int(nside) * int(nside)
         check(load().pisco_set_sky_device(self.ctx, int(nside), d_iquv, FLOAT64 if f64 else FLOAT32,
                                           stream or None), self.ctx, "set_sky_device")
 
@@ -300,6 +302,69 @@ class GPUConvolver:
         v = ctypes.c_longlong()
         check(load().pisco_count_pairs(self.ctx, ctypes.byref(v)), self.ctx, "count_pairs")
         return int(v.value)
+
+    # ---- adjoint
+    def set_beam_device(self, nside: int, npix: int, d_ab: int, f64: bool = False,
+                        stream: int = 0) -> None:
+        check(load().pisco_set_beam_device(self.ctx, int(nside), int(npix), d_ab,
+                                           FLOAT64 if f64 else FLOAT32, stream or None),
+              self.ctx, "set_beam_device")
+
+    def adjoint_device(self, d_ga: int, d_gb: int, g_f64: bool, d_gsky: int, d_gbeam: int,
+                       out_f64: bool = False, deterministic: bool = True, begin: int = 0,
+                       n: int | None = None, stream: int = 0) -> None:
+        n = self._n - begin if n is None else n
+        check(load().pisco_adjoint_device(self.ctx, begin, n, d_ga, d_gb,
+                                          FLOAT64 if g_f64 else FLOAT32, d_gsky or None,
+                                          d_gbeam or None, FLOAT64 if out_f64 else FLOAT32,
+                                          1 if deterministic else 0, stream or None),
+              self.ctx, "adjoint_device")
+
+    def adjoint(self, g_a: np.ndarray, g_b: np.ndarray, deterministic: bool = True,
+                out_f64: bool = True):
+        """Host-array adjoint: returns dL/d(I, Q, U, V) as a 4 x npix array."""
+        dt = _dtype_code(g_a)
+        g_a = np.ascontiguousarray(g_a)
+        g_b = np.ascontiguousarray(g_b, dtype=g_a.dtype)
+        npix = self._npix_sky
+        out = np.zeros((4, npix), np.float64 if out_f64 else np.float32)
+        check(load().pisco_adjoint(self.ctx, _ptr(g_a), _ptr(g_b), dt, *[_ptr(out[k]) for k in range(4)],
+                                   FLOAT64 if out_f64 else FLOAT32, 1 if deterministic else 0),
+              self.ctx, "adjoint")
+        return out
+
+    # ---- batched multi-detector forward
+    def set_beam_slot(self, slot: int, beam: "PolBeam") -> None:
+        a = [np.ascontiguousarray(x, dtype=np.float32) for x in beam.aBeams]
+        b = [np.ascontiguousarray(x, dtype=np.float32) for x in beam.bBeams]
+        check(load().pisco_set_beam_slot(self.ctx, int(slot), beam.nside, beam.nPixels,
+                                         ptr_array([x.ctypes.data for x in a]),
+                                         ptr_array([x.ctypes.data for x in b]), FLOAT32),
+              self.ctx, "set_beam_slot")
+
+    @staticmethod
+    def det_descs(dets) -> ctypes.Array:
+        """dets: iterable of (slot, n, d_ra, d_dec, d_pa, d_tod_a, d_tod_b)."""
+        dets = list(dets)
+        arr = (_lib.DetDesc * len(dets))()
+        for i, (slot, n, ra, dec, pa, ta, tb) in enumerate(dets):
+            arr[i] = _lib.DetDesc(int(slot), 0, int(n), ra, dec, pa, ta or None, tb or None)
+        return arr
+
+    def forward_batched(self, descs, out_f64: bool = False, chunk: int = 0, stream: int = 0) -> None:
+        check(load().pisco_forward_batched(self.ctx, descs, len(descs),
+                                           FLOAT64 if out_f64 else FLOAT32, int(chunk),
+                                           stream or None), self.ctx, "forward_batched")
+
+    def autotune_batched(self, descs, out_f64: bool = False, cache_path: str | None = None):
+        ch = ctypes.c_int()
+        ms = ctypes.c_double()
+        check(load().pisco_autotune_batched(self.ctx, descs, len(descs),
+                                            FLOAT64 if out_f64 else FLOAT32,
+                                            cache_path.encode() if cache_path else None,
+                                            ctypes.byref(ch), ctypes.byref(ms)),
+              self.ctx, "autotune_batched")
+        return int(ch.value), float(ms.value)
 
     def tuned_calibrate(self, begin: int = 0, n: int | None = None) -> float:
         """Worst FP32 decision error of the TUNED form as a fraction of its margin."""

@@ -1,0 +1,250 @@
+// adjoint.cu -- transpose of the TUNED forward: TOD residuals back-projected
+// onto the sky I/Q/U/V maps and (optionally) onto the beam maps.
+//
+// The forward is linear in the sky and in the beam:
+//   tod_a(s) = sum_p I a0 + Q (a1 c2 - a2 s2) + U (a2 c2 + a1 s2) + V a3
+//   tod_b(s) = sum_p I b0 + Q (-b1 c2 + b2 s2) + U (-b2 c2 - b1 s2) + V b3
+// (convolver.cpp:195-202 with the GPU's V term, cudaConv2.cu:204,214), so
+//   dL/dI(p) += ga a0 + gb b0,  dL/dQ(p) += ga (a1 c2 - a2 s2) + gb (-b1 c2 + b2 s2), ...
+//   dL/da0(b) += ga I, dL/da1(b) += ga (Q c2 + U s2), dL/da2(b) += ga (U c2 - Q s2), ...
+// for every pair (s, p) with beam pixel b, with the pair set and the beam
+// pixel of each pair taken by exactly the TUNED forward's geometry
+// (tuned_core.cuh), so the adjoint is the transpose of that operator.
+//
+// Accumulation, two variants:
+//  * ATOMIC: float atomics (vector float4 adds for the sky) -- fast, but the
+//    order of the additions, hence the last bits, varies run to run.
+//  * DETERMINISTIC: 64-bit fixed-point integer atomics.  Integer addition is
+//    associative, so the sums are bit-identical whatever the order.  The
+//    scale 2^S is set from a rigorous bound on any total (computed by fixed-
+//    order reductions), leaving 2^-62 of that bound as the resolution; the
+//    per-pixel error is at most (#contributions x 2^-S) / 2.
+#include <cuda_runtime.h>
+
+#include "tuned_core.cuh"
+
+namespace pisco {
+namespace {
+
+constexpr int kAW = 8;
+
+template <bool kFixed>
+struct Scatter {
+    float ga, gb;
+    float* gsky;                  // ATOMIC: float4-interleaved [npix][4]
+    unsigned long long* gsky_fx;  // DETERMINISTIC: int64 [npix][4]
+    float* gbeam;                 // ATOMIC: [npixB][8] (a.IQUV, b.IQUV) or null
+    unsigned long long* gbeam_fx;
+    const float4* sky;            // for the beam gradient
+    double ssky, sbeam;           // fixed-point scales 2^S
+
+    __device__ __forceinline__ static unsigned long long fx(double v, double scale)
+    {
+        return (unsigned long long)__double2ll_rn(v * scale);
+    }
+
+    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    {
+        const float gI = ga * B.a.x + gb * B.b.x;
+        const float gQ = ga * (B.a.y * c2 - B.a.z * s2) + gb * (-B.b.y * c2 + B.b.z * s2);
+        const float gU = ga * (B.a.z * c2 + B.a.y * s2) + gb * (-B.b.z * c2 - B.b.y * s2);
+        const float gV = ga * B.a.w + gb * B.b.w;
+        if (kFixed) {
+            unsigned long long* p = gsky_fx + 4ll * pix;
+            atomicAdd(p + 0, fx(gI, ssky));
+            atomicAdd(p + 1, fx(gQ, ssky));
+            atomicAdd(p + 2, fx(gU, ssky));
+            atomicAdd(p + 3, fx(gV, ssky));
+        } else {
+            atomicAdd(reinterpret_cast<float4*>(gsky) + pix, make_float4(gI, gQ, gU, gV));
+        }
+    }
+};
+
+// Sky and beam gradient: the beam pixel index is recovered as &B - base
+// (the action receives a reference to beam[bp] itself).
+template <bool kFixed>
+struct ScatterBeam {
+    float ga, gb;
+    const F8* beam_base;
+    const float4* sky;
+    float* gsky;
+    unsigned long long* gsky_fx;
+    float* gbeam;
+    unsigned long long* gbeam_fx;
+    double ssky, sbeam;
+    int want_sky;
+
+    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    {
+        if (want_sky) {
+            Scatter<kFixed> sc{ga, gb, gsky, gsky_fx, nullptr, nullptr, nullptr, ssky, sbeam};
+            sc.pair(pix, B, c2, s2);
+        }
+        const long long bp = &B - beam_base;
+        const float4 S = __ldg(&sky[pix]);
+        const float qa = S.y * c2 + S.z * s2, ua = S.z * c2 - S.y * s2;
+        const float v[8] = {ga * S.x, ga * qa, ga * ua, ga * S.w, gb * S.x, -gb * qa, -gb * ua, gb * S.w};
+        if (kFixed) {
+            unsigned long long* p = gbeam_fx + 8 * bp;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) atomicAdd(p + k, Scatter<kFixed>::fx(v[k], sbeam));
+        } else {
+            float4* p = reinterpret_cast<float4*>(gbeam) + 2 * bp;
+            atomicAdd(p, make_float4(v[0], v[1], v[2], v[3]));
+            atomicAdd(p + 1, make_float4(v[4], v[5], v[6], v[7]));
+        }
+    }
+};
+
+template <class Act>
+__global__ void __launch_bounds__(kAW * 32, 2) adjoint_kernel(AdjArgs a, Act proto)
+{
+    __shared__ tuned::WarpSmem sm[kAW];
+    const int lane = threadIdx.x & 31;
+    tuned::WarpSmem& S = sm[threadIdx.x >> 5];
+    const Hpx hs = hpx_make(a.nside_sky);
+    const Hpx hb = hpx_make(a.nside_beam);
+    const tuned::Beam B = {a.beam32, a.nside_beam, a.npix_beam, a.rho_max,
+                           (float)(1.7320508075688772 * a.nside_beam)};
+    const long long gw = (long long)blockIdx.x * kAW + (threadIdx.x >> 5);
+    const long long nw = (long long)gridDim.x * kAW;
+    unsigned long long nfall = 0;
+    float cmax = 0.0f;
+    Act act = proto;
+    for (long long i = gw; i < a.n; i += nw) {
+        const long long s = a.begin + i;
+        const double ga = a.g_f64 ? ((const double*)a.g_a)[i] : (double)((const float*)a.g_a)[i];
+        const double gb = a.g_f64 ? ((const double*)a.g_b)[i] : (double)((const float*)a.g_b)[i];
+        if (ga == 0.0 && gb == 0.0) continue;
+        act.ga = (float)ga;
+        act.gb = (float)gb;
+        tuned::sample<false>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], S, lane, a.err, act, nfall, cmax);
+    }
+    if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
+}
+
+// Fixed-order partial sums of |ga| + |gb| (one per block, then one block).
+__global__ void abs_sum_kernel(const void* ga, const void* gb, int f64, long long n, double* part)
+{
+    __shared__ double sh[256];
+    double v = 0.0;
+    for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += 256ll * gridDim.x) {
+        const double x = f64 ? ((const double*)ga)[i] : (double)((const float*)ga)[i];
+        const double y = f64 ? ((const double*)gb)[i] : (double)((const float*)gb)[i];
+        if (isfinite(x)) v += fabs(x);
+        if (isfinite(y)) v += fabs(y);
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// max |component| of a float array, fixed order (blocks -> one block).
+__global__ void abs_max_kernel(const float* x, long long n, double* part)
+{
+    __shared__ double sh[256];
+    double v = 0.0;
+    for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += 256ll * gridDim.x)
+        if (isfinite(x[i])) v = fmax(v, fabs((double)x[i]));
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void fold_kernel(double* part, int nb, int is_max)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double v = 0.0;
+    for (int i = 0; i < nb; ++i) v = is_max ? fmax(v, part[i]) : v + part[i];
+    part[0] = v;
+}
+
+__global__ void fixed_to_float_kernel(const unsigned long long* in, void* out, int out_f64,
+                                      long long n, double inv_scale)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = (double)(long long)in[i] * inv_scale;
+        if (out_f64) ((double*)out)[i] = v;
+        else ((float*)out)[i] = (float)v;
+    }
+}
+
+template <class K>
+int resident_blocks(K kernel, int threads)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0) != cudaSuccess ||
+        nb < 1)
+        nb = 1;
+    return nb;
+}
+
+template <class Act>
+cudaError_t launch_act(const AdjArgs& a, const Act& act, int sm_count, cudaStream_t st)
+{
+    const long long need = (a.n + kAW - 1) / kAW;
+    long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act>, kAW * 32);
+    adjoint_kernel<Act><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+constexpr int kRedBlocks = 256;
+
+cudaError_t launch_abs_sum(const void* ga, const void* gb, int f64, long long n, double* part,
+                           cudaStream_t st)
+{
+    abs_sum_kernel<<<kRedBlocks, 256, 0, st>>>(ga, gb, f64, n, part);
+    fold_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_abs_max(const float* x, long long n, double* part, cudaStream_t st)
+{
+    abs_max_kernel<<<kRedBlocks, 256, 0, st>>>(x, n, part);
+    fold_kernel<<<1, 32, 0, st>>>(part, kRedBlocks, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fixed_to_float(const unsigned long long* in, void* out, int out_f64, long long n,
+                                  double inv_scale, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    fixed_to_float_kernel<<<1024, 256, 0, st>>>(in, out, out_f64, n, inv_scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st)
+{
+    if (a.n <= 0) return cudaSuccess;
+    const bool beam = a.gbeam32 || a.gbeam_fx;
+    if (a.fixed) {
+        if (beam) {
+            ScatterBeam<true> act{0, 0, a.beam32, a.sky32, nullptr, a.gsky_fx, nullptr, a.gbeam_fx,
+                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr};
+            return launch_act(a, act, sm_count, st);
+        }
+        Scatter<true> act{0, 0, nullptr, a.gsky_fx, nullptr, nullptr, a.sky32, a.sky_scale, a.beam_scale};
+        return launch_act(a, act, sm_count, st);
+    }
+    if (beam) {
+        ScatterBeam<false> act{0, 0, a.beam32, a.sky32, a.gsky32, nullptr, a.gbeam32, nullptr,
+                               0.0, 0.0, a.gsky32 != nullptr};
+        return launch_act(a, act, sm_count, st);
+    }
+    Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0};
+    return launch_act(a, act, sm_count, st);
+}
+
+}  // namespace pisco

@@ -55,6 +55,12 @@ pisco_ctx::~pisco_ctx()
                     (void*)dec, (void*)pa, (void*)d_err, (void*)d_count, (void*)d_fallbacks,
                     (void*)out_dev})
         if (p) cudaFree(p);
+    for (auto& s : slots)
+        if (s.beam) cudaFree(s.beam);
+    for (void* p : {(void*)d_dets, (void*)d_items, (void*)d_queue, (void*)adj_sky32,
+                    (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red})
+        if (p) cudaFree(p);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (stream) cudaStreamDestroy(stream);
 }
 

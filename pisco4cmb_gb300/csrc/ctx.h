@@ -4,9 +4,15 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/pisco_gb300.h"
 #include "internal.h"
+
+namespace pisco {
+std::vector<BatchItem> make_items(const std::vector<BatchDet>& dets, const std::vector<double>& cost,
+                                  long long chunk);
+}
 
 struct pisco_ctx {
     pisco_run_config cfg{};
@@ -50,6 +56,37 @@ struct pisco_ctx {
     unsigned long long* d_fallbacks = nullptr;
     long long pairs = 0;
     bool pairs_valid = false;
+
+    // batched multi-detector forward
+    struct BeamSlot {
+        pisco::F8* beam = nullptr;
+        size_t cap = 0;
+        int nside = 0;
+        long npix = 0;
+        double rho_max = 0.0;
+    };
+    std::vector<BeamSlot> slots;
+    pisco::BatchDet* d_dets = nullptr;
+    size_t d_dets_cap = 0;
+    pisco::BatchItem* d_items = nullptr;
+    size_t d_items_cap = 0;
+    unsigned int* d_queue = nullptr;
+    // graph of the last batched launch (queue reset + kernel) and its key
+    cudaGraphExec_t graph_exec = nullptr;
+    std::string graph_key;
+    int batched_chunk = 0;  // last autotuned chunk (0 = not tuned)
+
+    // adjoint scratch
+    float* adj_sky32 = nullptr;
+    size_t adj_sky32_cap = 0;
+    float* adj_beam32 = nullptr;
+    size_t adj_beam32_cap = 0;
+    unsigned long long* adj_sky_fx = nullptr;
+    size_t adj_sky_fx_cap = 0;
+    unsigned long long* adj_beam_fx = nullptr;
+    size_t adj_beam_fx_cap = 0;
+    double* red = nullptr;
+    size_t red_cap = 0;
 
     ~pisco_ctx();
     pisco_status activate();

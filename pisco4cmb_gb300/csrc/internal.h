@@ -58,6 +58,72 @@ struct FwdArgs {
     unsigned long long* fallbacks;  // tuned form: pairs re-evaluated in FP64
 };
 
+// One detector pair of a batched launch, as the device sees it.
+struct BatchDet {
+    const F8* beam;
+    int nside_beam;
+    int npix_beam;
+    double rho_max;
+    float rscale;  // sqrt(3) * nside_beam
+    long long n;
+    const double* ra;
+    const double* dec;
+    const double* pa;
+    void* out_a;
+    void* out_b;
+};
+
+// One unit of the work queue: samples [begin, begin + count) of detector det.
+struct BatchItem {
+    int det;
+    int count;
+    long long begin;
+};
+
+struct BatchArgs {
+    int nside_sky;
+    const float4* sky32;
+    const BatchDet* dets;
+    int ndet;
+    const BatchItem* items;
+    int nitems;
+    unsigned int* queue;  // next item (reset to 0 before every launch)
+    int out_f64;
+    unsigned int* err;
+    unsigned long long* fallbacks;
+};
+
+struct AdjArgs {
+    int nside_sky;
+    const float4* sky32;  // needed for the beam gradient
+    int nside_beam;
+    int npix_beam;
+    const F8* beam32;
+    double rho_max;
+    long long begin, n;
+    const double* ra;
+    const double* dec;
+    const double* pa;
+    const void* g_a;  // dL/dTOD a, b (n values each)
+    const void* g_b;
+    int g_f64;
+    int fixed;                     // 1: fixed-point int64 accumulation
+    float* gsky32;                 // atomic: [npix][4] or null
+    unsigned long long* gsky_fx;   // fixed: [npix][4] or null
+    float* gbeam32;                // atomic: [npixB][8] or null
+    unsigned long long* gbeam_fx;  // fixed: [npixB][8] or null
+    double sky_scale, beam_scale;  // fixed-point scales 2^S
+    unsigned int* err;
+    unsigned long long* fallbacks;
+};
+
+cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st);
+cudaError_t launch_abs_sum(const void* ga, const void* gb, int f64, long long n, double* part,
+                           cudaStream_t st);
+cudaError_t launch_abs_max(const float* x, long long n, double* part, cudaStream_t st);
+cudaError_t launch_fixed_to_float(const unsigned long long* in, void* out, int out_f64, long long n,
+                                  double inv_scale, cudaStream_t st);
+
 // PLAIN (f64 = false) and FP64 (f64 = true) forms.
 cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaStream_t st);
 // TUNED form; returns cudaErrorNotSupported when the beam does not fit the
@@ -67,6 +133,9 @@ bool tuned_supported(int nside_beam, int npix_beam, double rho_max);
 // Same kernel with every FP32 decision also evaluated in FP64: writes the
 // worst |FP32 - FP64| / margin seen over the non-fallback pairs to *calib.
 cudaError_t launch_tuned_calibrate(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib);
+// Batched TUNED forward (fwd_batched.cu).
+int batched_grid(int sm_count);
+cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st);
 // Per-sample disc sizes (pairs) for the roofline byte model.
 cudaError_t launch_count_pairs(int nside_sky, double rho_max, long long n, const double* ra,
                                const double* dec, unsigned long long* total, int sm_count,

@@ -21,6 +21,7 @@ maps (reference ``scripts/create_cmb.py``), GRASP beams
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -130,11 +131,26 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
 
 def grf_sky(nside: int, config_id: int, rms_i: float = 100.0, rms_qu: float = 10.0,
             lmax: int | None = None, dtype=np.float32, device: str = "cpu") -> np.ndarray:
-    """4 x npix I, Q, U, V (V = 0) sky in microkelvin."""
+    """4 x npix I, Q, U, V (V = 0) sky in microkelvin.
+
+    Large skies are cached as .npy under $PISCO_SYNTH_CACHE (default
+    /tmp/pisco4cmb_gb300_synth) so repeated runs on one machine reuse them.
+    """
     npix = 12 * nside * nside
+    cache = None
+    if nside >= 256:
+        d = os.environ.get("PISCO_SYNTH_CACHE", "/tmp/pisco4cmb_gb300_synth")
+        cache = os.path.join(d, "sky_n%d_c%d_l%s_%g_%g.npy" % (nside, config_id, lmax, rms_i, rms_qu))
+        if os.path.exists(cache):
+            return np.load(cache).astype(dtype)
     sky = np.zeros((4, npix), np.float64)
     for k, rms in enumerate((rms_i, rms_qu, rms_qu)):
         sky[k] = rms * grf_map(nside, lmax, [SEED_BASE + config_id, 100 + k], device=device)
+    if cache:
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        tmp = cache + ".tmp%d" % os.getpid()
+        np.save(tmp, sky)
+        os.replace(tmp + ".npy" if not tmp.endswith(".npy") else tmp, cache)
     return sky.astype(dtype)
 
 
