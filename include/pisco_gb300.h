@@ -175,6 +175,41 @@ pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, 
                                     pisco_dtype out_dtype, const char* cache_path,
                                     int* chunk_out, double* ms_out);
 
+/* ---- allocation-free batched forward (no counterpart in the reference) --
+ * For callers that may not allocate device memory (real-time loops, host
+ * callbacks, services whose memory pool owns the whole GPU): the batched
+ * TUNED forward with every buffer supplied by the caller and its own
+ * working memory (work queue, descriptors, counters) in a fixed array of
+ * about 0.5 MB compiled into the library, shared by all calls.  No context;
+ * calls no allocator.  Synchronous (returns when the TOD is written).
+ * Limits: at most PISCO_NOALLOC_MAX_DETS detector pairs and at most
+ * PISCO_NOALLOC_MAX_ITEMS work items, sum over pairs of
+ * ceil(nsamples / chunk) -- raise chunk for long scans; beyond either limit
+ * the call returns PISCO_ERR_INVALID_ARGUMENT with the reason in
+ * pisco_last_error(NULL).  The first call on a device looks up the array's
+ * device address and should come before any stream capture on that device.
+ * Calls whose GPU work overlaps race on the shared array: serialise them. */
+#define PISCO_NOALLOC_MAX_DETS 128
+#define PISCO_NOALLOC_MAX_ITEMS 32768
+
+typedef struct pisco_noalloc_det {
+    int nside_beam;
+    long npix_beam;
+    const float* beam_ab; /* device, npix_beam x 8: a.I,Q,U,V, b.I,Q,U,V; 16-B aligned */
+    long long nsamples;
+    const double* ra; /* device FP64 pointing */
+    const double* dec;
+    const double* pa;
+    float* tod_a; /* device outputs (either may be NULL) */
+    float* tod_b;
+} pisco_noalloc_det;
+
+/* d_sky_iquv: device, 12 nside_sky^2 x 4 floats (I,Q,U,V), 16-B aligned.
+ * chunk: samples per work item (0 = 256). */
+pisco_status pisco_forward_batched_noalloc(int device, int nside_sky, const float* d_sky_iquv,
+                                           const pisco_noalloc_det* dets, int ndet, int chunk,
+                                           void* stream);
+
 /* ---- adjoint (no reference counterpart: PISCO has no gradient) --------- */
 /* ATOMIC: float atomics, fast, last bits vary run to run.
  * DETERMINISTIC: 64-bit fixed-point atomics with a scale from a rigorous

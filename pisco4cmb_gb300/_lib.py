@@ -68,6 +68,19 @@ class DetDesc(ctypes.Structure):
                 ("tod_a", ctypes.c_void_p), ("tod_b", ctypes.c_void_p)]
 
 
+class NoallocDet(ctypes.Structure):
+    """pisco_noalloc_det: one detector pair of the allocation-free batched forward."""
+
+    _fields_ = [("nside_beam", ctypes.c_int), ("npix_beam", ctypes.c_long),
+                ("beam_ab", ctypes.c_void_p), ("nsamples", ctypes.c_longlong),
+                ("ra", ctypes.c_void_p), ("dec", ctypes.c_void_p), ("pa", ctypes.c_void_p),
+                ("tod_a", ctypes.c_void_p), ("tod_b", ctypes.c_void_p)]
+
+
+NOALLOC_MAX_DETS = 128
+NOALLOC_MAX_ITEMS = 32768
+
+
 # every symbol the header declares: (name, restype, argtypes)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -97,6 +110,7 @@ SIGNATURES = [
     ("pisco_forward_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, _I, _P]),
     ("pisco_autotune_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, ctypes.c_char_p,
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    ("pisco_forward_batched_noalloc", _S, [_I, _I, _P, ctypes.POINTER(NoallocDet), _I, _I, _P]),
     ("pisco_set_beam_device", _S, [_P, _I, _L, _P, _I, _P]),
     ("pisco_adjoint_device", _S, [_P, _L, _L, _P, _P, _I, _P, _P, _I, _I, _P]),
     ("pisco_adjoint", _S, [_P, _P, _P, _I, _P, _P, _P, _P, _I, _I]),

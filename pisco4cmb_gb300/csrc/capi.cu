@@ -48,6 +48,11 @@ pisco_status cuda_fail(pisco_ctx* c, cudaError_t e, const char* what)
 
 }  // namespace
 
+namespace pisco {
+// Message for pisco_last_error(NULL) from entry points that have no context.
+void set_null_ctx_error(const char* msg) { g_create_error = msg; }
+}  // namespace pisco
+
 pisco_ctx::~pisco_ctx()
 {
     cudaSetDevice(device);
