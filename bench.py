@@ -65,12 +65,14 @@ def measured_peaks():
 
 
 def ncu_traffic_per_launch():
-    """DRAM bytes per launch of the tuned forward from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "tuned_forward_c2.json")
+    """DRAM bytes (read + write) per full-size launch of the tuned forward, from
+    the committed ncu summary (line 'dram_bytes_per_launch: <int>')."""
+    p = os.path.join(ROOT, "profiles", "tuned_forward_c2_dram_traffic.md")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return d.get("dram_bytes_per_launch_full_c2")
+            for line in f:
+                if line.strip().startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1].strip())
     return None
 
 
@@ -183,7 +185,14 @@ def cpu_sample_size(wl, threads: int, target_s: float):
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return 0
-    wl = make_workload("cpu", 200_000)
+    # input generation is not timed; the sky synthesis uses the GPU when there is one
+    try:
+        import torch
+
+        gen_dev = "cuda" if torch.cuda.is_available() else "cpu"
+    except Exception:  # noqa: BLE001
+        gen_dev = "cpu"
+    wl = make_workload(gen_dev, 200_000)
     threads = host_cores()
     n, kind = cpu_sample_size(wl, threads, 5.0)
     for _ in range(args.warmup):
@@ -293,6 +302,13 @@ def run_gpu_arm(args, rank, world, local):
     err = torch.cat([ta - fa, tb - fb])
     rms_err = torch.sqrt(torch.mean(err ** 2)).item() / rms
     max_err = torch.max(torch.abs(err)).item() / rms
+    # worst FP32 decision error (fraction of the FP64 margin) and exactness
+    # of the TUNED disc on a bounded prefix
+    m_cal = min(n, args.accuracy_samples // 5)
+    worst_frac, tuned_pairs = conv.tuned_calibrate(0, m_cal, with_pairs=True)
+    conv.update_scan(Scan(m_cal, wl["ra"][:m_cal], wl["dec"][:m_cal], wl["pa"][:m_cal]))
+    exact_pairs = conv.count_pairs()
+    conv.update_scan(Scan(n, wl["ra"], wl["dec"], wl["pa"]))
 
     # e2e through the C ABI with pinned host buffers, host<->device copies inside
     ra_h = torch.from_numpy(wl["ra"]).pin_memory()
@@ -369,7 +385,10 @@ def run_gpu_arm(args, rank, world, local):
             "plain": {"value": plain_sps, "unit": "samples/s", "sample": m_plain,
                       "tuned_over_plain": value / world / plain_sps},
             "accuracy": {"rms_err_vs_fp64": rms_err, "max_err_vs_fp64": max_err,
-                         "sample": m_acc, "relative_to": "TOD rms"},
+                         "sample": m_acc, "relative_to": "TOD rms",
+                         "worst_fp32_decision_error_over_margin": worst_frac,
+                         "tuned_disc_pairs_equal_exact": tuned_pairs == exact_pairs,
+                         "calibration_sample": m_cal},
             "macs_per_s": pairs * 8 * world * args.steps / t_total,
             "fp64_fallback_pairs_per_step": fallbacks,
             "cpu_baseline": cpu,
@@ -380,6 +399,241 @@ def run_gpu_arm(args, rank, world, local):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+    return 0
+
+
+# ------------------------------------------------------------------ other workloads
+def _events():
+    import torch
+
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _study_stream():
+    """Makes a fresh (non-default) torch stream current and returns its
+    handle: torch events then record on the stream the library launches on.
+    (A null handle would select the library context's own stream, which
+    torch's default-stream events do not see.)"""
+    import torch
+
+    st = torch.cuda.Stream()
+    torch.cuda.set_stream(st)
+    return st.cuda_stream
+
+
+def _gaussian_beam(nside_beam, radius_deg, fwhm_deg, ell, nside_sky, epsilon=0.01, phi0=0.0):
+    from pisco4cmb_gb300 import PolBeam, beam_npix_for_radius, synth
+
+    npb = beam_npix_for_radius(nside_beam, math.radians(radius_deg))
+    beam = PolBeam(nside_beam, npb, epsilon, "p")
+    fx, fy = synth.elliptical_fwhm(fwhm_deg, ell)
+    beam.make_unpol_gaussian_elliptical_beams(fx, fy, phi0)
+    beam.build(nside_sky)
+    return beam
+
+
+def run_c3_precision(args):
+    """Precision study: FP32/FP64-pointing TUNED vs all-FP64 on the GPU (and vs
+    the CPU FP64 oracle on a small prefix), pole-heavy scan."""
+    import torch
+
+    import oracle
+    from pisco4cmb_gb300 import GPUConvolver, Scan, Sky, synth
+
+    w = synth.WORKLOADS[3]
+    t0 = time.time()
+    sky = synth.grf_sky(w["nside_sky"], 3, lmax=w["lmax"], dtype=np.float32, device="cuda")
+    beam = _gaussian_beam(w["nside_beam"], w["radius_deg"], w["fwhm_deg"], w["ellipticity"],
+                          w["nside_sky"])
+    n = args.samples or w["nsamples"]
+    ra, dec, pa = synth.pole_heavy_scan(n, 3)
+    gen = time.time() - t0
+    conv = GPUConvolver(form="tuned")
+    conv.update_sky(Sky(w["nside_sky"], sky[0], sky[1], sky[2], None))
+    conv.update_beam(beam)
+    conv.update_scan(Scan(n, ra, dec, pa))
+    pairs = conv.count_pairs()
+    out = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(2)]
+    cs = _study_stream()
+    conv.forward_device(out[0].data_ptr(), out[1].data_ptr(), out_f64=True, form="tuned", stream=cs)
+    conv.sync()
+    e0, e1 = _events()
+    e0.record()
+    conv.forward_device(out[0].data_ptr(), out[1].data_ptr(), out_f64=True, form="tuned", stream=cs)
+    e1.record()
+    torch.cuda.synchronize()
+    t_tuned = e0.elapsed_time(e1) / 1e3
+    tuned = [x.cpu().numpy() for x in out]
+    fb = conv.last_fallbacks()
+    m = min(n, args.fp64_samples)
+    ref = [torch.empty(m, dtype=torch.float64, device="cuda") for _ in range(2)]
+    e0.record()
+    conv.forward_device(ref[0].data_ptr(), ref[1].data_ptr(), out_f64=True, n=m, form="fp64",
+                        stream=cs)
+    e1.record()
+    torch.cuda.synchronize()
+    t_fp64 = e0.elapsed_time(e1) / 1e3
+    ref = [x.cpu().numpy() for x in ref]
+    rms = float(np.sqrt(np.mean(np.concatenate(ref) ** 2)))
+    err = np.concatenate([tuned[0][:m] - ref[0], tuned[1][:m] - ref[1]])
+    pole = np.abs(np.abs(dec[:m]) - np.pi / 2) <= np.radians(1.0)
+    errp = np.concatenate([(tuned[0][:m] - ref[0])[pole], (tuned[1][:m] - ref[1])[pole]])
+    worst = conv.tuned_calibrate(0, min(n, 20000))
+    # CPU FP64 oracle on a small prefix (every 10th sample is a pole pointing)
+    mc = min(n, args.cpu_samples)
+    ba, bb = beam.planes()
+    oa, ob = oracle.convolve_f64(ra[:mc], dec[:mc], pa[:mc], w["nside_sky"],
+                                 sky.astype(np.float64), w["nside_beam"], ba.astype(np.float64),
+                                 bb.astype(np.float64), nthreads=host_cores())
+    errc = np.concatenate([tuned[0][:mc] - oa, tuned[1][:mc] - ob])
+    errf = np.concatenate([ref[0][:mc] - oa, ref[1][:mc] - ob])
+    line = {"workload": "c3_precision_nside2048_beam1deg", "nsamples": n, "pairs": pairs,
+            "tuned_samples_per_s": n / t_tuned, "fp64_gpu_samples_per_s": m / t_fp64,
+            "fp64_fallback_pairs": fb, "worst_fp32_decision_error_over_margin": worst,
+            "tuned_vs_fp64_gpu": {"rms": float(np.sqrt(np.mean(err ** 2)) / rms),
+                                  "max": float(np.abs(err).max() / rms), "samples": m,
+                                  "pole_samples": int(pole.sum()),
+                                  "pole_max": float(np.abs(errp).max() / rms) if errp.size else None},
+            "tuned_vs_cpu_fp64_oracle": {"rms": float(np.sqrt(np.mean(errc ** 2)) / rms),
+                                         "max": float(np.abs(errc).max() / rms), "samples": mc},
+            "fp64_gpu_vs_cpu_fp64_oracle": {"max": float(np.abs(errf).max() / rms),
+                                            "samples": mc},
+            "relative_to": "TOD rms", "input_gen_s": gen}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_c4_batched(args):
+    """48 uneven detector pairs: one autotuned persistent launch vs sequential."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, Scan, Sky, synth
+
+    w = synth.WORKLOADS[4]
+    nss = w["nside_sky"]
+    sky = synth.grf_sky(nss, 4, dtype=np.float32, device="cuda")
+    dets = synth.c4_detectors()
+    conv = GPUConvolver(form="tuned")
+    conv.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    rows, keep, beams, scans = [], [], [], []
+    for d, p in enumerate(dets):
+        beam = _gaussian_beam(w["nside_beam"], p["radius_deg"], p["radius_deg"] / 2.5,
+                              p["ellipticity"], nss, w["epsilon"])
+        conv.set_beam_slot(d, beam)
+        ra, dec, pa = synth.sweep_scan(p["nsamples"], 4, stream=100 + d)
+        ra, dec = synth.offset_pointing(ra, dec, p["dx_deg"], p["dy_deg"])
+        t = [torch.tensor(x, device="cuda") for x in (ra, dec, pa)]
+        o = [torch.empty(p["nsamples"], device="cuda") for _ in range(2)]
+        keep.append((t, o))
+        beams.append(beam)
+        scans.append((ra, dec, pa))
+        rows.append((d, p["nsamples"], t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(),
+                     o[0].data_ptr(), o[1].data_ptr()))
+    descs = conv.det_descs(rows)
+    total = sum(p["nsamples"] for p in dets)
+    cache = os.path.join(os.environ.get("PISCO_TUNE_CACHE", "/tmp"), "pisco_autotune.json")
+    chunk, tune_ms = conv.autotune_batched(descs, cache_path=cache)
+    cs = _study_stream()
+    for _ in range(2):
+        conv.forward_batched(descs, stream=cs)
+    conv.sync()
+    e0, e1 = _events()
+    e0.record()
+    for _ in range(args.steps):
+        conv.forward_batched(descs, stream=cs)
+    e1.record()
+    conv.sync()
+    torch.cuda.synchronize()
+    t_batched = e0.elapsed_time(e1) / 1e3 / args.steps
+    batched_out = [[o.cpu().numpy() for o in k[1]] for k in keep]
+    # sequential single-detector launches (TUNED and PLAIN), one context each pair
+    seq = {}
+    for form in ("tuned", "plain"):
+        c = GPUConvolver(form=form)
+        c.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+        tt = 0.0
+        same = True
+        frac = 1.0 if form == "tuned" else args.plain_fraction
+        nseq = 0
+        for d, p in enumerate(dets):
+            m = max(1, int(p["nsamples"] * frac))
+            c.update_beam(beams[d])
+            ra, dec, pa = scans[d]
+            c.update_scan(Scan(m, ra[:m], dec[:m], pa[:m]))
+            oa = torch.empty(m, device="cuda")
+            ob = torch.empty(m, device="cuda")
+            e0.record()
+            c.forward_device(oa.data_ptr(), ob.data_ptr(), stream=cs)
+            e1.record()
+            torch.cuda.synchronize()
+            tt += e0.elapsed_time(e1) / 1e3
+            nseq += m
+            if form == "tuned":
+                same &= bool(np.array_equal(oa.cpu().numpy(), batched_out[d][0][:m]))
+        seq[form] = {"samples_per_s": nseq / tt, "samples": nseq, "bit_identical_to_batched":
+                     same if form == "tuned" else None}
+        c.close()
+    line = {"workload": "c4_batched_48pairs_nside512", "ndet": len(dets), "total_samples": total,
+            "autotuned_chunk": chunk, "autotune_best_ms": tune_ms,
+            "batched_graph_samples_per_s": total / t_batched, "batched_ms": t_batched * 1e3,
+            "sequential_tuned": seq["tuned"], "sequential_plain": seq["plain"],
+            "batched_over_sequential_tuned": (total / t_batched) / seq["tuned"]["samples_per_s"],
+            "batched_over_sequential_plain": (total / t_batched) / seq["plain"]["samples_per_s"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_c5_adjoint(args):
+    """Adjoint (sky and beam gradients) time vs forward time, both variants."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, Sky, synth
+
+    w = synth.WORKLOADS[5]
+    nss, nsb = w["nside_sky"], w["nside_beam"]
+    sky = synth.grf_sky(nss, 5, dtype=np.float32, device="cuda")
+    beam = _gaussian_beam(nsb, w["radius_deg"], w["fwhm_deg"], w["ellipticity"], nss)
+    n = w["ndet"] * (args.samples or w["nsamples"])
+    ra, dec, pa = synth.sweep_scan(n, 5)
+    conv = GPUConvolver(form="tuned")
+    conv.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    conv.update_beam(beam)
+    t = [torch.tensor(x, device="cuda") for x in (ra, dec, pa)]
+    conv.set_scan_device(n, *[x.data_ptr() for x in t])
+    pairs = conv.count_pairs()
+    ta = torch.empty(n, device="cuda")
+    tb = torch.empty(n, device="cuda")
+    ga = torch.randn(n, device="cuda")
+    gb = torch.randn(n, device="cuda")
+    gsky = torch.empty((12 * nss * nss, 4), device="cuda")
+    gbeam = torch.empty((beam.nPixels, 8), device="cuda")
+    e0, e1 = _events()
+
+    def timeit(fn, reps=args.steps):
+        fn()
+        conv.sync()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        conv.sync()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    cs = _study_stream()
+    t_fwd = timeit(lambda: conv.forward_device(ta.data_ptr(), tb.data_ptr(), form="tuned", stream=cs))
+    res = {}
+    for det in (True, False):
+        for with_beam in (False, True):
+            key = ("deterministic" if det else "atomic") + ("_sky_and_beam" if with_beam else "_sky")
+            res[key] = timeit(lambda: conv.adjoint_device(
+                ga.data_ptr(), gb.data_ptr(), False, gsky.data_ptr(),
+                gbeam.data_ptr() if with_beam else 0, deterministic=det, stream=cs))
+    line = {"workload": "c5_adjoint_nside256_beam4deg", "nsamples": n, "pairs": pairs,
+            "forward_ms": t_fwd * 1e3,
+            "adjoint_ms": {k: v * 1e3 for k, v in res.items()},
+            "adjoint_over_forward": {k: v / t_fwd for k, v in res.items()}}
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -394,12 +648,24 @@ def main():
     ap.add_argument("--accuracy-samples", type=int, default=50_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                    help="c2 = the headline line; c3/c4/c5 print their own study lines")
+    ap.add_argument("--fp64-samples", type=int, default=200_000)
+    ap.add_argument("--cpu-samples", type=int, default=2_000)
+    ap.add_argument("--plain-fraction", type=float, default=0.05)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = env_rank()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.workload != "c2":
+        import torch
+
+        torch.cuda.set_device(local)
+        if args.samples == 2_000_000:
+            args.samples = 0  # the workload's own sample count
+        return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 

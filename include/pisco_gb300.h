@@ -132,8 +132,11 @@ pisco_status pisco_last_fallbacks(pisco_ctx* ctx, long long* fallbacks);
 /* Diagnostic (no reference counterpart): runs the TUNED form on samples
  * [begin, begin+n) with each FP32 pixel decision also evaluated in FP64 and
  * returns the worst FP32 error as a fraction of the FP64 re-evaluation
- * margin (must stay well below 1).  Outputs are discarded. */
-pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* worst_fraction);
+ * margin (must stay well below 1), and (if tuned_pairs is not NULL) the
+ * number of disc pairs the TUNED disc evaluation produced (must equal
+ * pisco_count_pairs over the same samples).  Outputs are discarded. */
+pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* worst_fraction,
+                                   long long* tuned_pairs);
 
 /* ---- batched multi-detector forward ------------------------------------ */
 /* One detector pair of a batched forward.  Device pointers: FP64 pointing

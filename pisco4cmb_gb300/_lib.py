@@ -105,7 +105,8 @@ SIGNATURES = [
     ("pisco_sync", _S, [_P]),
     ("pisco_count_pairs", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_last_fallbacks", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
-    ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double)]),
+    ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_set_beam_slot", _S, [_P, _I, _I, _L, _PP, _PP, _I]),
     ("pisco_forward_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, _I, _P]),
     ("pisco_autotune_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, ctypes.c_char_p,

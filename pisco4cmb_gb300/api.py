@@ -366,13 +366,15 @@ class GPUConvolver:
               self.ctx, "autotune_batched")
         return int(ch.value), float(ms.value)
 
-    def tuned_calibrate(self, begin: int = 0, n: int | None = None) -> float:
-        """Worst FP32 decision error of the TUNED form as a fraction of its margin."""
+    def tuned_calibrate(self, begin: int = 0, n: int | None = None, with_pairs: bool = False):
+        """Worst FP32 decision error of the TUNED form as a fraction of its
+        margin (and, with_pairs, the TUNED disc's pair count)."""
         n = self._n - begin if n is None else n
         v = ctypes.c_double()
-        check(load().pisco_tuned_calibrate(self.ctx, begin, n, ctypes.byref(v)), self.ctx,
-              "tuned_calibrate")
-        return float(v.value)
+        p = ctypes.c_longlong()
+        check(load().pisco_tuned_calibrate(self.ctx, begin, n, ctypes.byref(v), ctypes.byref(p)),
+              self.ctx, "tuned_calibrate")
+        return (float(v.value), int(p.value)) if with_pairs else float(v.value)
 
     def last_fallbacks(self) -> int:
         v = ctypes.c_longlong()

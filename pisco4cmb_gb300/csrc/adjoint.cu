@@ -28,8 +28,11 @@ namespace {
 
 constexpr int kAW = 8;
 
+// Queued pairs are redone after the sample has moved on, so the weights
+// (ga, gb) of their sample travel in its slot (stash / deferred).
 template <bool kFixed>
 struct Scatter {
+    static constexpr bool kSums = false;
     float ga, gb;
     float* gsky;                  // ATOMIC: float4-interleaved [npix][4]
     unsigned long long* gsky_fx;  // DETERMINISTIC: int64 [npix][4]
@@ -43,12 +46,28 @@ struct Scatter {
         return (unsigned long long)__double2ll_rn(v * scale);
     }
 
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    __device__ __forceinline__ void stash(tuned::Pend& p) const
     {
-        const float gI = ga * B.a.x + gb * B.b.x;
-        const float gQ = ga * (B.a.y * c2 - B.a.z * s2) + gb * (-B.b.y * c2 + B.b.z * s2);
-        const float gU = ga * (B.a.z * c2 + B.a.y * s2) + gb * (-B.b.z * c2 - B.b.y * s2);
-        const float gV = ga * B.a.w + gb * B.b.w;
+        p.ga = ga;
+        p.gb = gb;
+    }
+    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, float c2,
+                                            float s2, float&, float&) const
+    {
+        scatter(p.ga, p.gb, pix, B, c2, s2);
+    }
+    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2) const
+    {
+        scatter(ga, gb, pix, B, c2, s2);
+    }
+
+    __device__ __forceinline__ void scatter(float wa, float wb, int pix, const F8& B, float c2,
+                                           float s2) const
+    {
+        const float gI = wa * B.a.x + wb * B.b.x;
+        const float gQ = wa * (B.a.y * c2 - B.a.z * s2) + wb * (-B.b.y * c2 + B.b.z * s2);
+        const float gU = wa * (B.a.z * c2 + B.a.y * s2) + wb * (-B.b.z * c2 - B.b.y * s2);
+        const float gV = wa * B.a.w + wb * B.b.w;
         if (kFixed) {
             unsigned long long* p = gsky_fx + 4ll * pix;
             atomicAdd(p + 0, fx(gI, ssky));
@@ -65,6 +84,7 @@ struct Scatter {
 // (the action receives a reference to beam[bp] itself).
 template <bool kFixed>
 struct ScatterBeam {
+    static constexpr bool kSums = false;
     float ga, gb;
     const F8* beam_base;
     const float4* sky;
@@ -75,16 +95,32 @@ struct ScatterBeam {
     double ssky, sbeam;
     int want_sky;
 
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    __device__ __forceinline__ void stash(tuned::Pend& p) const
+    {
+        p.ga = ga;
+        p.gb = gb;
+    }
+    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, float c2,
+                                            float s2, float&, float&) const
+    {
+        scatter(p.ga, p.gb, pix, B, c2, s2);
+    }
+    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2) const
+    {
+        scatter(ga, gb, pix, B, c2, s2);
+    }
+
+    __device__ __forceinline__ void scatter(float wa, float wb, int pix, const F8& B, float c2,
+                                           float s2) const
     {
         if (want_sky) {
-            Scatter<kFixed> sc{ga, gb, gsky, gsky_fx, nullptr, nullptr, nullptr, ssky, sbeam};
+            const Scatter<kFixed> sc{wa, wb, gsky, gsky_fx, nullptr, nullptr, nullptr, ssky, sbeam};
             sc.pair(pix, B, c2, s2);
         }
         const long long bp = &B - beam_base;
         const float4 S = __ldg(&sky[pix]);
         const float qa = S.y * c2 + S.z * s2, ua = S.z * c2 - S.y * s2;
-        const float v[8] = {ga * S.x, ga * qa, ga * ua, ga * S.w, gb * S.x, -gb * qa, -gb * ua, gb * S.w};
+        const float v[8] = {wa * S.x, wa * qa, wa * ua, wa * S.w, wb * S.x, -wb * qa, -wb * ua, wb * S.w};
         if (kFixed) {
             unsigned long long* p = gbeam_fx + 8 * bp;
 #pragma unroll
@@ -98,20 +134,21 @@ struct ScatterBeam {
 };
 
 template <class Act>
-__global__ void __launch_bounds__(kAW * 32, 2) adjoint_kernel(AdjArgs a, Act proto)
+__global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(AdjArgs a, Act proto)
 {
     __shared__ tuned::WarpSmem sm[kAW];
     const int lane = threadIdx.x & 31;
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
     const Hpx hs = hpx_make(a.nside_sky);
     const Hpx hb = hpx_make(a.nside_beam);
-    const tuned::Beam B = {a.beam32, a.nside_beam, a.npix_beam, a.rho_max,
-                           (float)(1.7320508075688772 * a.nside_beam)};
+    const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
     const long long gw = (long long)blockIdx.x * kAW + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kAW;
-    unsigned long long nfall = 0;
+    unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
     Act act = proto;
+    tuned::Queue Q{0, 0};
+    const tuned::Out none{nullptr, nullptr, 0, 0};
     for (long long i = gw; i < a.n; i += nw) {
         const long long s = a.begin + i;
         const double ga = a.g_f64 ? ((const double*)a.g_a)[i] : (double)((const float*)a.g_a)[i];
@@ -119,8 +156,10 @@ __global__ void __launch_bounds__(kAW * 32, 2) adjoint_kernel(AdjArgs a, Act pro
         if (ga == 0.0 && gb == 0.0) continue;
         act.ga = (float)ga;
         act.gb = (float)gb;
-        tuned::sample<false>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], S, lane, a.err, act, nfall, cmax);
+        tuned::sample<false>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], none, S, Q, lane, a.err, act,
+                             nfall, cmax, npairs);
     }
+    tuned::flush(hs, S, Q, lane, a.err, act);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
 }
 

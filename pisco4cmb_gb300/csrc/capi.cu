@@ -595,7 +595,8 @@ pisco_status pisco_last_fallbacks(pisco_ctx* c, long long* fallbacks)
     return PISCO_OK;
 }
 
-pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* worst)
+pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* worst,
+                                   long long* tuned_pairs)
 {
     if (!c || !worst) return PISCO_ERR_INVALID_ARGUMENT;
     if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
@@ -605,9 +606,9 @@ pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* wor
         return fail(c, PISCO_ERR_UNSUPPORTED, "beam outside the tuned form's domain");
     pisco_status st = c->activate();
     if (st != PISCO_OK) return st;
-    float* d = nullptr;
-    CK(cudaMalloc(&d, sizeof(float)), "calib buffer");
-    cudaMemsetAsync(d, 0, sizeof(float), c->stream);
+    float* d = nullptr;  // {worst fraction, pad, u64 disc pairs of the TUNED disc}
+    CK(cudaMalloc(&d, 16), "calib buffer");
+    cudaMemsetAsync(d, 0, 16, c->stream);
     FwdArgs a{};
     a.nside_sky = c->nside_sky;
     a.sky32 = c->sky32;
@@ -623,12 +624,15 @@ pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* wor
     a.err = c->d_err;
     a.fallbacks = c->d_fallbacks;
     cudaError_t e = launch_tuned_calibrate(a, c->sm_count, c->stream, d);
-    float v = 0.0f;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&v, d, sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, d, 16, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(c, e, "calibration");
-    *worst = v;
+    *worst = v[0];
+    unsigned long long pairs = 0;
+    std::memcpy(&pairs, &v[2], sizeof(pairs));
+    if (tuned_pairs) *tuned_pairs = (long long)pairs;
     return c->check_device();
 }
 

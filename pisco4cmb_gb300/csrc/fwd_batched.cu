@@ -6,7 +6,8 @@
 // focal plane of uneven detectors (beam radii 1-5 deg, 10k-1M samples) then
 // leaves the GPU idle in every tail.  Here the host cuts every detector's
 // samples into chunks, orders the chunks longest-first (estimated pairs),
-// and one kernel whose warps pull chunks with one atomic each runs them all.
+// and one kernel whose blocks pull chunks with one atomic each runs them all
+// (the 8 warps of a block share a chunk, sample by sample).
 // The launch (queue reset + kernel) is captured once in a CUDA graph and
 // replayed while the same detector set is resubmitted.  The chunk size is
 // chosen by the autotuner (pisco_autotune_batched) and cached per workload
@@ -36,41 +37,44 @@ namespace {
 
 constexpr int kBW = 8;  // warps per block
 
-__global__ void __launch_bounds__(kBW * 32, 2) batched_kernel(BatchArgs a)
+// A block pulls one item at a time and its warps take the item's samples
+// round-robin, so the warps of an SM work on neighbouring samples (whose
+// discs overlap) at the same moment, as in the single-detector launch.
+__global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(BatchArgs a)
 {
     __shared__ tuned::WarpSmem sm[kBW];
+    __shared__ int s_item[2];
     const int lane = threadIdx.x & 31;
-    tuned::WarpSmem& S = sm[threadIdx.x >> 5];
+    const int warp = threadIdx.x >> 5;
+    tuned::WarpSmem& S = sm[warp];
     const Hpx hs = hpx_make(a.nside_sky);
-    unsigned long long nfall = 0;
+    unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
     tuned::Gather g;
     g.sky = a.sky32;
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = (int)atomicAdd(a.queue, 1u);
-        item = __shfl_sync(tuned::kFull, item, 0);
+    tuned::Queue Q{0, 0};
+    for (int round = 0;; ++round) {
+        // double-buffered: a slot is rewritten only after the next barrier,
+        // which every thread reaches after reading it
+        if (threadIdx.x == 0) s_item[round & 1] = (int)atomicAdd(a.queue, 1u);
+        __syncthreads();
+        const int item = s_item[round & 1];
         if (item >= a.nitems) break;
         const BatchItem it = a.items[item];
         if (it.det < 0 || it.det >= a.ndet) {
-            tuned::record(a.err, kCheckQueue);
+            if (threadIdx.x == 0) tuned::record(a.err, kCheckQueue);
             continue;
         }
         const BatchDet d = a.dets[it.det];
         const Hpx hb = hpx_make(d.nside_beam);
-        const tuned::Beam B = {d.beam, d.nside_beam, d.npix_beam, d.rho_max, d.rscale};
-        for (long long s = it.begin; s < it.begin + it.count; ++s) {
-            g.reset();
-            double ta = CUDART_NAN, tb = CUDART_NAN;
-            if (tuned::sample<false>(hs, hb, B, d.ra[s], d.dec[s], d.pa[s], S, lane, a.err, g,
-                                     nfall, cmax))
-                g.total(ta, tb);
-            if (lane == 0) {
-                tuned::store_out(d.out_a, a.out_f64, s, ta);
-                tuned::store_out(d.out_b, a.out_f64, s, tb);
-            }
+        const tuned::Beam B = tuned::make_beam(d.beam, d.nside_beam, d.npix_beam, d.rho_max);
+        for (long long s = it.begin + warp; s < it.begin + it.count; s += kBW) {
+            const tuned::Out o{d.out_a, d.out_b, s, a.out_f64};
+            tuned::sample<false>(hs, hb, B, d.ra[s], d.dec[s], d.pa[s], o, S, Q, lane, a.err, g,
+                                 nfall, cmax, npairs);
         }
     }
+    tuned::flush(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
 }
 

@@ -17,7 +17,7 @@ namespace {
 constexpr int kTW = 8;
 
 template <bool kCalib>
-__global__ void __launch_bounds__(kTW * 32, 2)
+__global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
     tuned_kernel(FwdArgs a, float rscale, float* calib)
 {
     __shared__ tuned::WarpSmem sm[kTW];
@@ -25,30 +25,30 @@ __global__ void __launch_bounds__(kTW * 32, 2)
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
     const Hpx hs = hpx_make(a.nside_sky);
     const Hpx hb = hpx_make(a.nside_beam);
-    const tuned::Beam B = {a.beam32, a.nside_beam, a.npix_beam, a.rho_max, rscale};
+    const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    (void)rscale;
     const long long gw = (long long)blockIdx.x * kTW + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kTW;
-    unsigned long long nfall = 0;
+    unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
     tuned::Gather g;
     g.sky = a.sky32;
+    tuned::Queue Q{0, 0};
     for (long long i = gw; i < a.n; i += nw) {
         const long long s = a.begin + i;
-        g.reset();
-        double ta = CUDART_NAN, tb = CUDART_NAN;
-        if (tuned::sample<kCalib>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], S, lane, a.err, g, nfall,
-                                  cmax))
-            g.total(ta, tb);
-        if (lane == 0) {
-            tuned::store_out(a.out_a, a.out_f64, i, ta);
-            tuned::store_out(a.out_b, a.out_f64, i, tb);
-        }
+        const tuned::Out o{a.out_a, a.out_b, i, a.out_f64};
+        tuned::sample<kCalib>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane, a.err, g, nfall,
+                              cmax, npairs);
     }
+    tuned::flush(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
     if (kCalib && calib) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) cmax = fmaxf(cmax, __shfl_xor_sync(tuned::kFull, cmax, o));
-        if (lane == 0) atomicMax((int*)calib, __float_as_int(cmax));
+        if (lane == 0) {
+            atomicMax((int*)calib, __float_as_int(cmax));
+            atomicAdd(reinterpret_cast<unsigned long long*>(calib + 2), npairs);
+        }
     }
 }
 

@@ -312,7 +312,16 @@ struct DiscPlan {
     bool all_sky;
 };
 
+PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius, double cosr);
+
 PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius)
+{
+    return disc_plan(h, theta, phi, radius, radius >= kPi ? 0.0 : cos(radius));
+}
+
+// Same, with cos(radius) supplied by the caller (hoisted out of a loop over
+// pointings); it must be cos(radius) as evaluated on the same device.
+PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius, double cosr)
 {
     DiscPlan p;
     theta = fmodulo(theta, kTwoPi);
@@ -330,7 +339,7 @@ PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius)
         p.z0 = p.xa = p.cosr = 0.0;
         return p;
     }
-    p.cosr = cos(radius);
+    p.cosr = cosr;
     p.z0 = cos(theta);
     p.xa = PD_DIV(1.0, sqrt(PD_MUL(PD_SUB(1.0, p.z0), PD_ADD(1.0, p.z0))));
     double rlat1 = PD_SUB(theta, radius);

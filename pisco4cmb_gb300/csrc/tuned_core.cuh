@@ -2,16 +2,31 @@
 // single-detector forward (fwd_tuned.cu), the batched multi-detector forward
 // (fwd_batched.cu) and the adjoint (adjoint.cu).
 //
-// For one sample, a warp evaluates the HEALPix query_disc rings in FP64 (the
-// same code as the PLAIN form, so the disc is identical), rounds per-ring
-// small-offset constants to FP32 once, and strides the disc pairs across
-// lanes.  Per pair, FP32 only: longitude offset from a per-ring anchor pixel,
-// cancellation-free boresight-frame components, the beam grid's polar-cap
-// indices and exp(2i chi) as a product of unit phasors.  Any of the three
-// floor decisions lying within the margin of an integer, and any pair within
-// 2e-6 rad of the boresight, is queued and redone 32 at a time with the FP64
-// chain of the PLAIN form (hpx.cuh pair_beam_pixel), so every pair lands on
-// the same beam pixel as in the PLAIN form.
+// For one sample, a warp evaluates the HEALPix query_disc rings, one ring per
+// lane, rounds per-ring small-offset constants to FP32 once, and strides the
+// disc pairs across lanes.  Per pair, FP32 only: longitude offset from a
+// per-ring anchor pixel, cancellation-free boresight-frame components, the
+// beam grid's polar-cap indices and exp(2i chi) as a product of unit
+// phasors.  Any of the three floor decisions lying within the margin of an
+// integer, and any pair within 2e-6 rad of the boresight, is queued and redone
+// with the FP64 chain of the PLAIN form (hpx.cuh pair_beam_pixel), so every
+// pair lands on the same beam pixel as in PLAIN.
+//
+// The queue outlives the sample: each entry names a per-warp slot holding its
+// sample's FP64 frame and output, and the warp redoes 32 entries at a time,
+// whichever samples they came from (a sample queues about four pairs in a
+// thousand, so a per-sample drain would run the long FP64 chain with a few
+// lanes active).  The re-evaluated contributions of a sample are added in
+// queue order, one lane per sample, into an FP64 sum, and its TOD is written
+// (main-pass total + that sum) when its last entry is done: the result does
+// not depend on where the drains cut the queue, hence not on the other
+// samples of the warp.
+//
+// Disc edge: per ring, x and ysq of the HEALPix edge formula are formed in
+// FP64 with exactly HEALPix's rounding, the edge angle atan2(sqrt(ysq), x) is
+// taken in FP32, and the two floor decisions use FP64 positions; an edge
+// within the FP32 angle's error bound of a pixel boundary is recomputed with
+// the FP64 formula (disc_ring), so the disc is HEALPix query_disc's exactly.
 //
 // Geometry, with the pixel at ring height z (s = sqrt(1 - z^2)), longitude
 // offset D from the boresight (z0, s0) and h = 1 - cos D:
@@ -22,15 +37,27 @@
 //   alpha = atan2(u, v),  exp(2i chi) = exp(2i beta) exp(2i alpha) exp(2i psi)
 // (sphtrigo.cpp:27-54 rewritten in small-offset form).
 //
-// The per-pair work is handed to an Action:
+// The per-pair work is handed to an Action (Gather below, Scatter in
+// adjoint.cu):
+//   kSums                     true: per-sample sums, TOD written per sample
+//   void reset(), total(a, b) main-pass sums (kSums)
 //   void pair(int pix, const F8& beam, float c2, float s2)
-// (c2, s2 = cos 2chi, sin 2chi).
+//   void stash(Pend&)         per-sample data a queued pair needs later
+//   void deferred(const Pend&, int pix, const F8& beam, float c2, float s2,
+//                 float& ta, float& tb)      a re-evaluated pair
+// (c2, s2 = cos 2chi, sin 2chi; `beam` refers to the beam array element).
 #pragma once
 
 #include <math_constants.h>
 
 #include "hpx.cuh"
 #include "internal.h"
+
+// Minimum resident 256-thread blocks per SM requested from the compiler for
+// the kernels built on this core (caps their registers).
+#ifndef PISCO_TUNED_MINB
+#define PISCO_TUNED_MINB 2
+#endif
 
 namespace pisco {
 namespace tuned {
@@ -46,42 +73,97 @@ constexpr float kMarginRel = 1.2e-6f;
 // (rho <= 1e-6, sphtrigo.cpp:40-48) and are done in FP64.
 constexpr float kTinyQ = 4.0e-12f;
 
-struct Batch {
-    int incl[32];
-    int cnt[32];
-    int n1[32];
-    int s1[32];
-    int s2[32];
-    int b1[32];
-    int b2[32];
-    int nr[32];
-    float dc[32];
-    float dphi[32];
-    float si[32];
-    float Di[32];
-    float Ki[32];
-    float Zs[32];
-    float Wz[32];
-    float Pp[32];
+// One disc ring of the current batch: FP32 offset constants and the pixel
+// range(s), 64 bytes, read with four 16-byte loads.
+struct alignas(16) RingC {
+    float dc, dphi, si, Di;  // anchor offset, pixel spacing, s, sin(dec - dec0)
+    float Ki, Zs, Wz, Pp;    // 1 - cos(dec - dec0), s z0, s0 z, s s0
+    int s1, s2, b1, b2;      // range starts, anchor offsets of the ranges
+    int n1, nr, incl, cnt;   // first range length, ring pixels, inclusive scan, pixels
 };
 
-// Per-warp shared state: one ring batch and the FP64 re-evaluation queue.
-struct WarpSmem {
-    Batch b;
-    int q[kQCap];
+// Samples in flight per warp (a sample keeps its slot until its queued
+// pairs are done).
+constexpr int kPend = 16;
+
+// A sample whose queued pairs may not all be re-evaluated yet.
+struct alignas(16) Pend {
+    Hpx hb;                  // beam grid
+    double ra, dec, psi;     // FP64 frame (psi = -pa)
+    double main_a, main_b;   // main-pass totals
+    double fb_a, fb_b;       // re-evaluated pairs, summed in queue order
+    const F8* beam;
+    void* out_a;
+    void* out_b;
+    long long idx;           // output index
+    float ga, gb;            // adjoint weights
+    int npix_beam;
+    int left;                // queued entries not yet re-evaluated
+    int open;                // main pass still running
+    int f64;                 // output type
 };
+
+// Per-warp shared state: one ring batch, the samples in flight and the FP64
+// re-evaluation queue (sky pixel, slot).
+struct WarpSmem {
+    RingC r[32];
+    Pend p[kPend];
+    int q[kQCap];
+    unsigned char qs[kQCap];
+    float ta[32], tb[32];
+};
+
+// Warp-uniform queue state, in registers.
+struct Queue {
+    int n;    // queued entries (< 32 between samples)
+    int cur;  // next slot
+};
+
+// Where one sample's TOD goes.
+struct Out {
+    void* a;
+    void* b;
+    long long idx;
+    int f64;
+};
+
+__device__ __forceinline__ void store_out(void* out, int f64, long long i, double v)
+{
+    if (!out) return;
+    if (f64) ((double*)out)[i] = v;
+    else ((float*)out)[i] = (float)v;
+}
+
+__device__ __forceinline__ void finalize(const Pend& P)
+{
+    store_out(P.out_a, P.f64, P.idx, P.main_a + P.fb_a);
+    store_out(P.out_b, P.f64, P.idx, P.main_b + P.fb_b);
+}
 
 struct Beam {
     const F8* beam;
     int nside;
     int npix;
     double rho_max;
+    double cosr;   // cos(rho_max), evaluated on the device
     float rscale;  // sqrt(3) * nside
 };
 
+__device__ __forceinline__ Beam make_beam(const F8* beam, int nside, int npix, double rho_max)
+{
+    Beam b;
+    b.beam = beam;
+    b.nside = nside;
+    b.npix = npix;
+    b.rho_max = rho_max;
+    b.cosr = rho_max >= kPi ? 0.0 : cos(rho_max);
+    b.rscale = (float)(1.7320508075688772 * (double)nside);
+    return b;
+}
+
 struct Frame {
     double ra, dec, psi;
-    float s0, z0, sps, cps, c2p, s2p;
+    float s0, sps, cps, c2p, s2p;
 };
 
 __device__ __forceinline__ void record(unsigned int* err, unsigned int code)
@@ -98,86 +180,287 @@ __device__ __forceinline__ void two_sum(float& s, float& c, float x)
     c += e;
 }
 
+// x within m of an integer (x - rint(x) is exact for |x| < 2^23).
 __device__ __forceinline__ bool near_int(float x, float m)
 {
-    const float f = x - floorf(x);
-    return f < m || f > 1.0f - m;
+    return fabsf(x - rintf(x)) < m;
 }
 
-// FP64 chain of the PLAIN form for one queued pair.
-template <class Action>
-__device__ __forceinline__ void fallback_pair(const Hpx& hs, const Hpx& hb, const Beam& B, int pix,
-                                           const Frame& F, unsigned int* err, Action& act)
+// 1/x by the MUFU reciprocal approximation (relative error below 2^-22);
+// used only for values, never for an index decision.
+__device__ __forceinline__ float rcp_approx(float x)
 {
-    double rho, sig, chi;
-    const long long bp = pair_beam_pixel(hs, hb, pix, F.ra, F.dec, F.psi, &rho, &sig, &chi);
-    if (bp >= B.npix) return;
-    if (bp < 0) {
-        record(err, kCheckBeamIndex);
-        return;
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The disc's pixel range(s) on one ring: FP32 edge angle, FP64 positions,
+// exact FP64 HEALPix formula (disc_ring) whenever an edge decision is within
+// the FP32 angle's error of a pixel boundary.  Same result as disc_ring.
+__device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan& p, long long ring,
+                                                   double z, const RingInfo& ri)
+{
+    RingSpan s = {0, 0, 0, 0};
+    if (ring < p.full_lo || ring > p.full_hi) return s;
+    if (p.all_sky || ring < p.ring_lo || ring > p.ring_hi) {
+        s.start1 = ri.start;
+        s.n1 = ri.npix;
+        return s;
     }
-    act.pair(pix, B.beam[bp], (float)cos(2.0 * chi), (float)sin(2.0 * chi));
+    const double x = PD_MUL(PD_SUB(p.cosr, PD_MUL(z, p.z0)), p.xa);
+    const double ysq = PD_SUB(PD_SUB(1.0, PD_MUL(z, z)), PD_MUL(x, x));
+    if (!(ysq > 0.0)) return s;  // no intersection (HEALPix: dphi = 0, ring skipped)
+    const float de = atan2f(sqrtf((float)ysq), (float)x);
+    const double shift = ri.shifted ? 0.5 : 0.0;
+    const double fr = (double)ri.npix * kInvTwoPi;
+    const double vlo = fr * (p.phi - (double)de) - shift;
+    const double vhi = fr * (p.phi + (double)de) - shift;
+    // |de - atan2(sqrt(ysq), x)| <= 3e-7 de (FP32 rounding of x, ysq and atan2f)
+    const double m = fr * (4e-7 * (double)de) + 1e-9;
+    const double flo = vlo - floor(vlo), fhi = vhi - floor(vhi);
+    if (!(de > 0.0f) || flo < m || flo > 1.0 - m || fhi < m || fhi > 1.0 - m)
+        return disc_ring(h, p, ring);
+    long long lo = (long long)floor(vlo) + 1;
+    long long hi = (long long)floor(vhi);
+    if (lo > hi) return s;
+    if (hi >= ri.npix) {
+        lo -= ri.npix;
+        hi -= ri.npix;
+    }
+    if (lo < 0) {
+        s.start1 = ri.start;
+        s.n1 = hi + 1;
+        s.start2 = ri.start + lo + ri.npix;
+        s.n2 = -lo;
+    } else {
+        s.start1 = ri.start + lo;
+        s.n1 = hi - lo + 1;
+    }
+    return s;
 }
 
-// Processes one sample; returns false (and does nothing) for a non-finite
-// pointing.  nfall counts queued pairs (lane 0 only); cmax (kCalib) is the
-// worst FP32 decision error over the non-queued pairs, in units of the margin.
-template <bool kCalib, class Action>
-__device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam& B, double ra,
-                                       double dec, double pa, WarpSmem& S, int lane,
-                                       unsigned int* err, Action& act,
-                                       unsigned long long& nfall, float& cmax)
+// Redoes the first m (<= 32, <= Q.n) queued pairs with the FP64 chain of the
+// PLAIN form, one per lane; credits each to its sample (serially, in queue
+// order, by the first lane of each run of one slot's entries), writes the TOD
+// of every sample left with nothing queued, and drops the m entries.
+template <class Action>
+__device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& Q, int lane,
+                                      unsigned int* err, Action& act)
 {
-    Batch& W = S.b;
-    int* Q = S.q;
+    float ta = 0.0f, tb = 0.0f;
+    int slot = -1;
+    if (lane < m) {
+        slot = S.qs[lane];
+        const Pend& P = S.p[slot];
+        const int pix = S.q[lane];
+        double rho, sig, chi;
+        const long long bp = pair_beam_pixel(hs, P.hb, pix, P.ra, P.dec, P.psi, &rho, &sig, &chi);
+        if (bp < 0)
+            record(err, kCheckBeamIndex);
+        else if (bp < P.npix_beam)
+            act.deferred(P, pix, P.beam[bp], (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+    }
+    if (Action::kSums) {
+        S.ta[lane] = ta;
+        S.tb[lane] = tb;
+    }
+    __syncwarp();
+    if (lane < m && (lane == 0 || S.qs[lane - 1] != slot)) {
+        Pend& P = S.p[slot];
+        int k = lane;
+        if (Action::kSums) {
+            double a = P.fb_a, b = P.fb_b;
+            do {
+                a += (double)S.ta[k];
+                b += (double)S.tb[k];
+                ++k;
+            } while (k < m && S.qs[k] == slot);
+            P.fb_a = a;
+            P.fb_b = b;
+        } else {
+            do ++k;
+            while (k < m && S.qs[k] == slot);
+        }
+        P.left -= k - lane;
+        if (Action::kSums && P.left == 0 && !P.open) finalize(P);
+    }
+    // move the rest (<= 32 entries: the queue holds < 64) to the front
+    const int rest = Q.n - m;
+    int vq = 0, vs = 0;
+    if (lane < rest) {
+        vq = S.q[m + lane];
+        vs = S.qs[m + lane];
+    }
+    __syncwarp();
+    if (lane < rest) {
+        S.q[lane] = vq;
+        S.qs[lane] = (unsigned char)vs;
+    }
+    __syncwarp();
+    Q.n = rest;
+}
+
+// Redoes every queued pair (at a sample boundary, where fewer than 32 are
+// queued): all slots are free afterwards.  Called once more before a warp
+// leaves the kernel.
+template <class Action>
+__device__ __forceinline__ void flush(const Hpx& hs, WarpSmem& S, Queue& Q, int lane,
+                                      unsigned int* err, Action& act)
+{
+    if (Q.n > 0) drain(hs, Q.n, S, Q, lane, err, act);
+}
+
+// sin(x) and 1 - cos(x): Taylor series for |x| <= 0.5 (truncation below
+// 3e-11 relative), CUDA sincosf beyond.
+__device__ __forceinline__ void sin_versin(float x, float& sn, float& h)
+{
+    if (fabsf(x) <= 0.5f) {
+        const float x2 = x * x;
+        sn = x * fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 2.75573192e-6f, -1.98412698e-4f),
+                                        8.33333333e-3f), -1.66666667e-1f), 1.0f);
+        h = x2 * fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 2.75573192e-7f, -2.48015873e-5f),
+                                        1.38888889e-3f), -4.16666667e-2f), 0.5f);
+    } else {
+        float cs;
+        sincosf(x, &sn, &cs);
+        h = (cs > 0.0f) ? (sn * sn) / (1.0f + cs) : 1.0f - cs;
+    }
+}
+
+// atan2(y, x) / (pi/2) for y, x >= 0, in [0, 1]: the arctangent of the
+// ratio min/max by the minimax polynomial of Abramowitz & Stegun 4.4.49
+// (|error| <= 2e-8 on [0, 1]; 1e-7 when evaluated in FP32), reflected for
+// y > x.  y = x = 0 gives 0 (such pairs are re-done in FP64 anyway).
+__device__ __forceinline__ float quarter_turns(float y, float x)
+{
+    const bool swap = y > x;
+    const float mn = swap ? x : y, mx = swap ? y : x;
+    const float t = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
+    const float t2 = t * t;
+    float p = 0.0028662257f;
+    p = fmaf(p, t2, -0.0161657367f);
+    p = fmaf(p, t2, 0.0429096138f);
+    p = fmaf(p, t2, -0.0752896400f);
+    p = fmaf(p, t2, 0.1065626393f);
+    p = fmaf(p, t2, -0.1420889944f);
+    p = fmaf(p, t2, 0.1999355085f);
+    p = fmaf(p, t2, -0.3333314528f);
+    p = fmaf(p, t2, 1.0f);
+    const float a = t * p * 0.63661977236758134f;  // atan(t) / (pi/2)
+    return swap ? 1.0f - a : a;
+}
+
+// Processes one sample.  A non-finite pointing gives NaN TOD (kSums) and no
+// pairs.  With kSums the TOD is written to `o` now, or by the drain that
+// redoes the sample's last queued pair.  nfall counts queued pairs and npairs
+// the disc pairs (lane 0 only); cmax (kCalib) is the worst FP32 decision
+// error over the non-queued pairs, in units of the margin.
+template <bool kCalib, class Action>
+__device__ __forceinline__ void sample(const Hpx& hs, const Hpx& hb, const Beam& B, double ra,
+                                       double dec, double pa, const Out& o, WarpSmem& S,
+                                       Queue& Qs, int lane, unsigned int* err, Action& act,
+                                       unsigned long long& nfall, float& cmax,
+                                       unsigned long long& npairs)
+{
+    RingC* W = S.r;
     const unsigned lt_mask = (1u << lane) - 1u;
     Frame F;
     F.ra = ra;
     F.dec = dec;
     F.psi = -pa;
-    if (!(isfinite(F.ra) && isfinite(F.dec) && isfinite(F.psi))) return false;
-    const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, F.dec), F.ra, B.rho_max);
-    const double z0d = sin(F.dec), s0d = cos(F.dec);
+    if (!(isfinite(F.ra) && isfinite(F.dec) && isfinite(F.psi))) {
+        if (Action::kSums && lane == 0) {
+            store_out(o.a, o.f64, o.idx, CUDART_NAN);
+            store_out(o.b, o.f64, o.idx, CUDART_NAN);
+        }
+        return;
+    }
+    // claim the next slot; one still waiting on queued pairs is freed by
+    // redoing the whole queue
+    const int slot = Qs.cur;
+    Qs.cur = slot + 1 == kPend ? 0 : slot + 1;
+    if (S.p[slot].left > 0) flush(hs, S, Qs, lane, err, act);
+    if (lane == 0) {
+        Pend& Ps = S.p[slot];
+        Ps.hb = hb;
+        Ps.ra = F.ra;
+        Ps.dec = F.dec;
+        Ps.psi = F.psi;
+        Ps.fb_a = Ps.fb_b = 0.0;
+        Ps.beam = B.beam;
+        Ps.out_a = o.a;
+        Ps.out_b = o.b;
+        Ps.idx = o.idx;
+        Ps.npix_beam = B.npix;
+        Ps.left = 0;
+        Ps.open = 1;
+        Ps.f64 = o.f64;
+        act.stash(Ps);
+    }
+    __syncwarp();
+    if constexpr (Action::kSums) act.reset();
+    const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, F.dec), F.ra, B.rho_max, B.cosr);
+    // Boresight frame.  The reference chain (sphtrigo.cpp:29-35) takes dec as
+    // given; for cos(dec) < 0 the same point is (pi - dec, ra + pi), and the
+    // chain's north direction then points the other way: its alpha is the
+    // normalised frame's + pi, hence its sigma is - pi, while beta and
+    // exp(2i chi) are unchanged.  So the geometry runs in the normalised frame
+    // (s0 >= 0) with (sin psi, cos psi) negated, which adds exactly pi to
+    // sigma.  ra is reduced mod 2pi (the anchor longitude of the rings).
+    double sdec, cdec;
+    sincos(F.dec, &sdec, &cdec);
+    const bool flip = cdec < 0.0;
+    const double z0d = sdec, s0d = flip ? -cdec : cdec;
+    const double phi_f = fmodulo(flip ? F.ra + kPi : F.ra, kTwoPi);
+    // psi phasors in FP64, rounded once: exp(2i psi) multiplies every pair
+    // of the sample, so its rounding error is coherent over the sample sum.
+    double spsi, cpsi;
+    sincos(F.psi, &spsi, &cpsi);
     F.s0 = (float)s0d;
-    F.z0 = (float)z0d;
-    F.sps = (float)sin(F.psi);
-    F.cps = (float)cos(F.psi);
-    F.c2p = (float)cos(2.0 * F.psi);
-    F.s2p = (float)sin(2.0 * F.psi);
-    int qn = 0;
+    F.sps = (float)(flip ? -spsi : spsi);
+    F.cps = (float)(flip ? -cpsi : cpsi);
+    F.c2p = (float)(cpsi * cpsi - spsi * spsi);
+    F.s2p = (float)(2.0 * spsi * cpsi);
 
     for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
         const long long ring = r0 + lane;
         int cnt = 0;
+        RingC rc;
+        rc.n1 = 0;
         if (ring <= P.full_hi) {
-            const RingSpan sp = disc_ring(hs, P, ring);
+            const RingInfo ri = ring_info(hs, ring);
+            const double z = ring2z(hs, ring);
+            const RingSpan sp = fast_disc_ring(hs, P, ring, z, ri);
             cnt = (int)(sp.n1 + sp.n2);
             if (cnt) {
-                const RingInfo ri = ring_info(hs, ring);
-                const double z = ring2z(hs, ring);
-                const double si = sqrt(PD_MUL(PD_SUB(1.0, z), PD_ADD(1.0, z)));
-                const double dz = z - z0d, ds = si - s0d;
-                const double n = (double)ri.npix;
-                const double dphi = kTwoPi / n;
+                // s = sqrt(1 - z^2) and 1/npix: FP32 seeds, one Newton step in FP64
+                const double omz = PD_MUL(PD_SUB(1.0, z), PD_ADD(1.0, z));
+                double rs = (double)rsqrtf((float)omz);
+                rs = rs * (1.5 - 0.5 * omz * rs * rs);
+                const double si = omz * rs;
+                const double nd = (double)ri.npix;
+                double rn = (double)__frcp_rn((float)ri.npix);
+                rn = rn * (2.0 - nd * rn);
+                const double dphi = kTwoPi * rn;
                 const double sh = ri.shifted ? 0.5 : 0.0;
-                const double jc = floor(P.phi / dphi - sh + 0.5);
-                W.dc[lane] = (float)((jc + sh) * dphi - P.phi);
-                W.dphi[lane] = (float)dphi;
-                W.si[lane] = (float)si;
-                W.Di[lane] = (float)(z * s0d - si * z0d);
-                W.Ki[lane] = (float)(0.5 * (dz * dz + ds * ds));
-                W.Zs[lane] = (float)(si * z0d);
-                W.Wz[lane] = (float)(s0d * z);
-                W.Pp[lane] = (float)(si * s0d);
-                W.nr[lane] = (int)ri.npix;
-                W.b1[lane] = (int)(sp.start1 - ri.start) - (int)jc;
-                W.b2[lane] = (int)(sp.start2 - ri.start) - (int)jc;
+                const double jc = floor(phi_f * (nd * kInvTwoPi) - sh + 0.5);
+                const double dz = z - z0d, ds = si - s0d;
+                rc.dc = (float)((jc + sh) * dphi - phi_f);
+                rc.dphi = (float)dphi;
+                rc.si = (float)si;
+                rc.Di = (float)(z * s0d - si * z0d);
+                rc.Ki = (float)(0.5 * (dz * dz + ds * ds));
+                rc.Zs = (float)(si * z0d);
+                rc.Wz = (float)(s0d * z);
+                rc.Pp = (float)(si * s0d);
+                rc.nr = (int)ri.npix;
+                rc.b1 = (int)(sp.start1 - ri.start) - (int)jc;
+                rc.b2 = (int)(sp.start2 - ri.start) - (int)jc;
             }
-            W.n1[lane] = (int)sp.n1;
-            W.s1[lane] = (int)sp.start1;
-            W.s2[lane] = (int)sp.start2;
-        } else {
-            W.n1[lane] = 0;
+            rc.n1 = (int)sp.n1;
+            rc.s1 = (int)sp.start1;
+            rc.s2 = (int)sp.start2;
         }
         int incl = cnt;
 #pragma unroll
@@ -186,9 +469,11 @@ __device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam&
             if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(kFull, incl, 31);
-        W.incl[lane] = incl;
-        W.cnt[lane] = cnt;
+        rc.incl = incl;
+        rc.cnt = cnt;
+        W[lane] = rc;
         __syncwarp();
+        if (lane == 0) npairs += (unsigned long long)total;
         int k = 0;  // lane slot (ring) owning the current pair; only moves forward
         const int iters = (total + 31) >> 5;
         for (int it = 0; it < iters; ++it) {
@@ -196,32 +481,34 @@ __device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam&
             bool fb = false;
             int pix = 0;
             if (t < total) {
-                while (W.incl[k] <= t) ++k;
-                const int u = t - (W.incl[k] - W.cnt[k]);
-                const int n1 = W.n1[k];
+                while (W[k].incl <= t) ++k;
+                const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
+                const int4 R3 = *reinterpret_cast<const int4*>(&W[k].n1);
+                const int u = t - (R3.z - R3.w);
                 int kk;
-                if (u < n1) {
-                    pix = W.s1[k] + u;
-                    kk = W.b1[k] + u;
+                if (u < R3.x) {
+                    pix = R2.x + u;
+                    kk = R2.z + u;
                 } else {
-                    pix = W.s2[k] + (u - n1);
-                    kk = W.b2[k] + (u - n1);
+                    pix = R2.y + (u - R3.x);
+                    kk = R2.w + (u - R3.x);
                 }
-                const int nr = W.nr[k];
+                const int nr = R3.y;
                 if (kk >= (nr >> 1)) kk -= nr;
                 if (kk < -(nr >> 1)) kk += nr;
                 if (pix < 0 || pix >= hs.npix) {
                     record(err, kCheckSkyIndex);
                 } else {
-                    const float dl = fmaf((float)kk, W.dphi[k], W.dc[k]);
-                    float sn, cs;
-                    sincosf(dl, &sn, &cs);
-                    const float h = (cs > 0.0f) ? (sn * sn) / (1.0f + cs) : 1.0f - cs;
-                    const float u_e = W.si[k] * sn;
-                    const float v_n = fmaf(W.Zs[k], h, W.Di[k]);
-                    const float q = fmaf(W.Pp[k], h, W.Ki[k]);
+                    const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
+                    const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
+                    const float dl = fmaf((float)kk, R0.y, R0.x);
+                    float sn, h;
+                    sin_versin(dl, sn, h);
+                    const float u_e = R0.z * sn;
+                    const float v_n = fmaf(R1.y, h, R0.w);
+                    const float q = fmaf(R1.w, h, R1.x);
                     const float nb = F.s0 * sn;
-                    const float db = fmaf(W.Wz[k], h, -W.Di[k]);
+                    const float db = fmaf(R1.z, h, -R0.w);
                     const float X = fmaf(u_e, F.sps, -v_n * F.cps);
                     const float Y = fmaf(u_e, F.cps, v_n * F.sps);
                     int qd;
@@ -233,8 +520,8 @@ __device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam&
                         if (X <= 0.0f) { qd = 2; yy = -Y; xx = -X; }
                         else { qd = 3; yy = X; xx = -Y; }
                     }
-                    const float tp = atan2f(yy, xx) * 0.63661977236758134f;
-                    const float r = B.rscale * sqrtf(q);
+                    const float tp = quarter_turns(yy, xx);
+                    const float r = B.rscale * (q * rsqrtf(q));
                     const float av = tp * r;
                     const float bv = (1.0f - tp) * r;
                     const int jp = (int)av, jm = (int)bv;
@@ -258,16 +545,15 @@ __device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam&
                     if (!fb) {
                         const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
                         if (bp >= 0 && bp < B.npix) {
-                            const float ia = 1.0f / fmaf(u_e, u_e, v_n * v_n);
-                            const float ca2 = (v_n * v_n - u_e * u_e) * ia;
-                            const float sa2 = 2.0f * u_e * v_n * ia;
-                            const float ib = 1.0f / fmaf(nb, nb, db * db);
-                            const float cb2 = (db * db - nb * nb) * ib;
-                            const float sb2 = 2.0f * nb * db * ib;
-                            const float cx = cb2 * ca2 - sb2 * sa2;
-                            const float sx = sb2 * ca2 + cb2 * sa2;
-                            act.pair(pix, B.beam[bp], cx * F.c2p - sx * F.s2p,
-                                     sx * F.c2p + cx * F.s2p);
+                            // exp(2i (beta + alpha)) = w^2 / |w|^2, w = (db + i nb)(v + i u),
+                            // then rotated by exp(2i psi)
+                            const float wr = fmaf(db, v_n, -nb * u_e);
+                            const float wi = fmaf(db, u_e, nb * v_n);
+                            const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
+                            const float er = fmaf(wr, wr, -wi * wi) * iw;
+                            const float ei = 2.0f * wr * wi * iw;
+                            act.pair(pix, B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
+                                     fmaf(ei, F.c2p, er * F.s2p));
                         }
                     }
                 }
@@ -275,42 +561,65 @@ __device__ __forceinline__ bool sample(const Hpx& hs, const Hpx& hb, const Beam&
             // queue near-edge pairs; redo them 32 at a time in FP64
             const unsigned mk = __ballot_sync(kFull, fb);
             if (mk) {
-                if (fb) Q[qn + __popc(mk & lt_mask)] = pix;
-                qn += __popc(mk);
-                nfall += (lane == 0) ? __popc(mk) : 0;
-                __syncwarp();
-                if (qn >= 32) {
-                    fallback_pair(hs, hb, B, Q[lane], F, err, act);
-                    __syncwarp();
-                    if (lane < qn - 32) Q[lane] = Q[32 + lane];
-                    qn -= 32;
-                    __syncwarp();
+                if (fb) {
+                    const int at = Qs.n + __popc(mk & lt_mask);
+                    S.q[at] = pix;
+                    S.qs[at] = (unsigned char)slot;
                 }
+                Qs.n += __popc(mk);
+                if (lane == 0) {
+                    nfall += __popc(mk);
+                    S.p[slot].left += __popc(mk);
+                }
+                __syncwarp();
+                if (Qs.n >= 32) drain(hs, 32, S, Qs, lane, err, act);
             }
         }
         __syncwarp();
     }
-    if (qn > 0) {
-        if (lane < qn) fallback_pair(hs, hb, B, Q[lane], F, err, act);
-        __syncwarp();
+    if constexpr (Action::kSums) {
+        double ta, tb;
+        act.total(ta, tb);
+        if (lane == 0) {
+            Pend& Ps = S.p[slot];
+            Ps.main_a = ta;
+            Ps.main_b = tb;
+            Ps.open = 0;
+            if (Ps.left == 0) finalize(Ps);
+        }
+    } else if (lane == 0) {
+        S.p[slot].open = 0;
     }
-    return true;
+    __syncwarp();
 }
 
 // Forward action: gather the sky, multiply by the beam, compensated sums.
 struct Gather {
+    static constexpr bool kSums = true;
     const float4* sky;
     float sa, ca, sb, cb;
     __device__ __forceinline__ void reset() { sa = ca = sb = cb = 0.0f; }
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    __device__ __forceinline__ void contrib(int pix, const F8& B, float c2, float s2, float& ta,
+                                           float& tb) const
     {
         const float4 S = __ldg(&sky[pix]);
-        const float ta = S.x * B.a.x + S.y * (B.a.y * c2 - B.a.z * s2) +
-                         S.z * (B.a.z * c2 + B.a.y * s2) + S.w * B.a.w;
-        const float tb = S.x * B.b.x + S.y * (-B.b.y * c2 + B.b.z * s2) +
-                         S.z * (-B.b.z * c2 - B.b.y * s2) + S.w * B.b.w;
+        ta = S.x * B.a.x + S.y * (B.a.y * c2 - B.a.z * s2) + S.z * (B.a.z * c2 + B.a.y * s2) +
+             S.w * B.a.w;
+        tb = S.x * B.b.x + S.y * (-B.b.y * c2 + B.b.z * s2) + S.z * (-B.b.z * c2 - B.b.y * s2) +
+             S.w * B.b.w;
+    }
+    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    {
+        float ta, tb;
+        contrib(pix, B, c2, s2, ta, tb);
         two_sum(sa, ca, ta);
         two_sum(sb, cb, tb);
+    }
+    __device__ __forceinline__ void stash(Pend&) const {}
+    __device__ __forceinline__ void deferred(const Pend&, int pix, const F8& B, float c2, float s2,
+                                            float& ta, float& tb) const
+    {
+        contrib(pix, B, c2, s2, ta, tb);
     }
     // warp total (fixed shuffle tree: deterministic)
     __device__ __forceinline__ void total(double& a, double& b) const
@@ -324,13 +633,6 @@ struct Gather {
         }
     }
 };
-
-__device__ __forceinline__ void store_out(void* out, int f64, long long i, double v)
-{
-    if (!out) return;
-    if (f64) ((double*)out)[i] = v;
-    else ((float*)out)[i] = (float)v;
-}
 
 }  // namespace tuned
 }  // namespace pisco

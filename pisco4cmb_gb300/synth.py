@@ -77,11 +77,12 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
     BIG = 1e100
     lam_mm = torch.full((R,), math.sqrt(1.0 / (4 * math.pi)), dtype=torch.float64, device=dev)
     e_mm = torch.zeros(R, dtype=torch.int32, device=dev)
-    lm1 = torch.zeros((M, R), dtype=torch.float64, device=dev)  # lambda_{l-1, m}
-    lm2 = torch.zeros((M, R), dtype=torch.float64, device=dev)  # lambda_{l-2, m}
+    # three rotating (m, ring) buffers: lambda_{l, m}, lambda_{l-1, m},
+    # lambda_{l-2, m}; step l reads and writes rows m <= l only
+    bufs = [torch.zeros((M, R), dtype=torch.float64, device=dev) for _ in range(3)]
     E = torch.zeros((M, R), dtype=torch.int32, device=dev)
     for l in range(0, M):
-        cur = torch.zeros((M, R), dtype=torch.float64, device=dev)
+        cur, lm1, lm2 = bufs[l % 3], bufs[(l - 1) % 3], bufs[(l - 2) % 3]
         if l >= 1:
             m = torch.arange(0, l - 1, dtype=torch.float64, device=dev)
             if m.numel():
@@ -111,7 +112,6 @@ def grf_map(nside: int, lmax: int | None, seed, device: str = "cpu",
             alm = torch.tensor(re + 1j * im, dtype=torch.complex128, device=dev)
             live = torch.where(E[: l + 1] == 0, cur[: l + 1], torch.zeros_like(cur[: l + 1]))
             F[: l + 1] += alm[:, None] * live
-        lm2, lm1 = lm1, cur
     # per ring: T(phi_j) = F_0 + 2 Re sum_{m>0} F_m e^{i m phi_j}
     out = np.empty(int(start[-1] + n_in[-1]), np.float64)
     mvec = torch.arange(M, dtype=torch.float64, device=dev)
@@ -213,7 +213,7 @@ WORKLOADS = {
             fwhm_deg=1.5, ellipticity=0.05, epsilon=0.01, nsamples=2_000_000, sky_dtype="float32"),
     3: dict(name="c3_precision_nside2048_beam1deg_4M", nside_sky=2048, nside_beam=4096,
             radius_deg=1.0, fwhm_deg=0.5, ellipticity=0.02, epsilon=0.01, nsamples=4_000_000,
-            sky_dtype="float32"),
+            sky_dtype="float32", lmax=2048),
     4: dict(name="c4_batched_48pairs_nside512", nside_sky=512, nside_beam=1024, ndet=48,
             epsilon=0.01, sky_dtype="float32"),
     5: dict(name="c5_adjoint_nside256", nside_sky=256, nside_beam=1024, radius_deg=4.0,

@@ -75,11 +75,67 @@ def test_tuned_decisions_within_margin(gpu, case, request):
     """Worst FP32 decision error of TUNED, as a fraction of its FP64 margin."""
     g = request.getfixturevalue(case)
     c = make_conv(g, form="tuned", ptg64=True)
-    worst = c.tuned_calibrate()
+    worst, tuned_pairs = c.tuned_calibrate(with_pairs=True)
     assert 0.0 <= worst < 0.5, worst
+    # the TUNED disc (FP32 edge angle, FP64 re-check) is HEALPix query_disc's exactly
+    assert tuned_pairs == c.count_pairs()
     a, b = run(c, g["ra"].size)
     nf = c.last_fallbacks()
     assert 0 <= nf < 0.02 * c.count_pairs()
+
+
+def test_tuned_disc_exact_on_random_pointings(gpu, oracle_mod):
+    """Pair counts of the TUNED disc equal the exact disc on random and
+    pole-grazing pointings, for several sky/beam resolutions."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky
+
+    rng = np.random.default_rng(77)
+    for nss, nsb, rdeg in ((16, 64, 9.0), (128, 512, 2.5), (512, 1024, 1.3), (2048, 4096, 0.6)):
+        npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(rdeg))
+        beam = PolBeam(nsb, npb, 0.0, "p")
+        beam.make_unpol_gaussian_elliptical_beams(rdeg / 2, rdeg / 2, 0.0)
+        beam.build(nss)
+        n = 4000
+        ra = rng.uniform(-1, 7, n)
+        dec = np.arcsin(rng.uniform(-1, 1, n))
+        dec[:400] = np.pi / 2 - rng.uniform(0, 1.5 * np.deg2rad(rdeg), 400)
+        dec[400:800] = -np.pi / 2 + rng.uniform(0, 1.5 * np.deg2rad(rdeg), 400)
+        c = GPUConvolver(form="tuned")
+        c.update_sky(Sky(nss, *np.zeros((3, 12 * nss * nss), np.float32), None))
+        c.update_beam(beam)
+        c.update_scan(Scan(n, ra, dec, rng.uniform(0, 3, n)))
+        worst, tp = c.tuned_calibrate(with_pairs=True)
+        assert tp == c.count_pairs() and worst < 0.5
+
+
+def test_tuned_unnormalised_pointing(gpu, oracle_mod):
+    """dec beyond +-90 deg and ra outside [0, 2pi): the reference chain takes
+    them as given; TUNED must agree with the FP64 form on the same inputs."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky
+
+    rng = np.random.default_rng(13)
+    nss, nsb = 64, 256
+    npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(5.0))
+    beam = PolBeam(nsb, npb, 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(2.0, 1.6, 40.0)
+    beam.build(nss)
+    n = 3000
+    ra = rng.uniform(-20, 20, n)
+    dec = rng.uniform(-2.5, 2.5, n)
+    pa = rng.uniform(-30, 30, n)
+    sky = rng.normal(size=(3, 12 * nss * nss)).astype(np.float32)
+    outs = {}
+    for form in ("tuned", "fp64"):
+        c = GPUConvolver(form=form)
+        c.update_sky(Sky(nss, *sky, None))
+        c.update_beam(beam)
+        c.update_scan(Scan(n, ra, dec, pa))
+        a = np.zeros(n)
+        b = np.zeros(n)
+        c.exec_convolution(a, b)
+        outs[form] = (a, b)
+    assert rel_max(outs["tuned"][0], outs["fp64"][0]) < 1e-6
+    assert rel_max(outs["tuned"][1], outs["fp64"][1]) < 1e-6
 
 
 def test_nonfinite_pointing_gives_nan(gpu, golden_c1):
