@@ -637,6 +637,54 @@ def run_c5_adjoint(args):
     return 0
 
 
+def run_order_study(args):
+    """Sky-ordered processing: the c2 TUNED forward on its sweep scan, on the
+    same samples shuffled (time order lost, as when many detectors or a
+    revisiting scan are concatenated), and on the shuffled samples in sky
+    order.  L2 flushed between timed steps."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, Scan, Sky
+
+    n = args.samples or 2_000_000
+    wl = make_workload("cuda", n)
+    sky = wl["sky"]
+    perm = np.random.default_rng(20261203).permutation(n)
+    cs = _study_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    e0, e1 = _events()
+    res = {}
+    for name, shuffled, order in (("sweep_scan_order", False, "scan"),
+                                  ("sweep_sky_order", False, "sky"),
+                                  ("shuffled_scan_order", True, "scan"),
+                                  ("shuffled_sky_order", True, "sky")):
+        ra, dec, pa = (wl[k][perm] if shuffled else wl[k] for k in ("ra", "dec", "pa"))
+        c = GPUConvolver(form="tuned")
+        c.update_sky(Sky(1024, sky[0], sky[1], sky[2], None))
+        c.update_beam(wl["beam"])
+        c.update_scan(Scan(n, ra, dec, pa))
+        c.set_sample_order(order)
+        a = torch.empty(n, device="cuda")
+        b = torch.empty(n, device="cuda")
+        for _ in range(2):  # the first call also sorts
+            c.forward_device(a.data_ptr(), b.data_ptr(), stream=cs)
+        c.sync()
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xff)
+            e0.record()
+            c.forward_device(a.data_ptr(), b.data_ptr(), stream=cs)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        res[name] = {"ms": float(np.median(ts)), "samples_per_s": n / (np.median(ts) / 1e3)}
+        c.close()
+    line = {"workload": "order_c2_nside1024_beam3deg", "nsamples": n, "timings": res,
+            "shuffled_sky_over_scan": res["shuffled_scan_order"]["ms"] / res["shuffled_sky_order"]["ms"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -648,8 +696,8 @@ def main():
     ap.add_argument("--accuracy-samples", type=int, default=50_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
-                    help="c2 = the headline line; c3/c4/c5 print their own study lines")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order"],
+                    help="c2 = the headline line; the others print their own study lines")
     ap.add_argument("--fp64-samples", type=int, default=200_000)
     ap.add_argument("--cpu-samples", type=int, default=2_000)
     ap.add_argument("--plain-fraction", type=float, default=0.05)
@@ -665,7 +713,8 @@ def main():
         torch.cuda.set_device(local)
         if args.samples == 2_000_000:
             args.samples = 0  # the workload's own sample count
-        return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint}[args.workload](args)
+        return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint,
+                "order": run_order_study}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 

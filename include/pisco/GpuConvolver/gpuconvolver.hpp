@@ -67,6 +67,13 @@ class GPUConvolver {
                             "GPUConvolver::exec_convolution");
     }
     void set_form(pisco_form f) { form = f; }
+    // PISCO_ORDER_SKY: each launch processes its samples sorted by sky cell
+    // (TOD unchanged, still in scan order); after configure_execution().
+    void set_sample_order(pisco_order order)
+    {
+        need_ctx();
+        pisco_detail::check(pisco_set_sample_order(ctx, order), ctx, "GPUConvolver::set_sample_order");
+    }
     pisco_ctx* handle() { return ctx; }
 
   private:

@@ -56,6 +56,13 @@ typedef enum pisco_form {
  * get_interpol block, convolver.cpp:162-185). */
 typedef enum pisco_interp { PISCO_BEAM_NEAREST = 0, PISCO_BEAM_BILINEAR = 1 } pisco_interp;
 
+/* Order in which a launch processes the samples of its range (no reference
+ * counterpart; the reference walks the scan in time order).  SKY sorts the
+ * range by a Z-order code of the pointing's sky cell so that concurrently
+ * running warps gather from overlapping disc footprints; TOD is written in
+ * scan order and is bit-identical in both orders. */
+typedef enum pisco_order { PISCO_ORDER_SCAN = 0, PISCO_ORDER_SKY = 1 } pisco_order;
+
 /* Mirrors CUDACONV::RunConfig (src/GpuConvolver/cuda/cudaConv2.h:13-26).
  * ptgPerConv is the host<->device pipelining chunk (samples); pixelsPerDisc
  * is accepted for compatibility (no disc lists are materialised);
@@ -106,6 +113,11 @@ pisco_status pisco_set_scan(pisco_ctx* ctx, long n, const void* ra, const void* 
 pisco_status pisco_set_scan_device(pisco_ctx* ctx, long n, const double* d_ra,
                                    const double* d_dec, const double* d_pa, void* stream);
 pisco_status pisco_set_interp(pisco_ctx* ctx, pisco_interp interp);
+/* Sample order of the context's forward and adjoint launches (default
+ * PISCO_ORDER_SCAN).  In SKY order the sort of a sample range runs on the
+ * launch's stream the first time the range is used after pisco_set_scan*,
+ * and is reused after that. */
+pisco_status pisco_set_sample_order(pisco_ctx* ctx, pisco_order order);
 
 /* ---- forward --------------------------------------------------------- */
 /* GPUConvolver::exec_convolution (gpuconvolver.cu:382-505) and
@@ -145,7 +157,8 @@ pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* w
  * (gpuconvolver.hpp:17-82); a focal plane is a loop over such objects. */
 typedef struct pisco_det_desc {
     int beam_slot; /* beam set with pisco_set_beam_slot */
-    int reserved;
+    int flags;     /* PISCO_DET_SKY_ORDER: process this pair's samples in sky
+                      order (sorted when the launch is captured) */
     long long nsamples;
     const double* ra;
     const double* dec;
@@ -153,6 +166,7 @@ typedef struct pisco_det_desc {
     void* tod_a;
     void* tod_b;
 } pisco_det_desc;
+#define PISCO_DET_SKY_ORDER 1
 
 /* Beam of one detector pair (PolBeam::aBeams / bBeams planes), kept in slot
  * `slot` (0 <= slot < 1024) for batched launches; same arguments as
@@ -182,8 +196,8 @@ pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, 
  * For callers that may not allocate device memory (real-time loops, host
  * callbacks, services whose memory pool owns the whole GPU): the batched
  * TUNED forward with every buffer supplied by the caller and its own
- * working memory (work queue, descriptors, counters) in a fixed array of
- * about 0.5 MB compiled into the library, shared by all calls.  No context;
+ * working memory (sky ring table, work queue, descriptors, counters) in a
+ * fixed array of about 2.6 MB compiled into the library, shared by all calls.  No context;
  * calls no allocator.  Synchronous (returns when the TOD is written).
  * Limits: at most PISCO_NOALLOC_MAX_DETS detector pairs and at most
  * PISCO_NOALLOC_MAX_ITEMS work items, sum over pairs of

@@ -59,10 +59,13 @@ class RunConfig(ctypes.Structure):
                          blockSizeY, ptgPerConv, pixelsPerDisc)
 
 
+PISCO_DET_SKY_ORDER = 1
+
+
 class DetDesc(ctypes.Structure):
     """pisco_det_desc: one detector pair of a batched forward (device pointers)."""
 
-    _fields_ = [("beam_slot", ctypes.c_int), ("reserved", ctypes.c_int),
+    _fields_ = [("beam_slot", ctypes.c_int), ("flags", ctypes.c_int),
                 ("nsamples", ctypes.c_longlong), ("ra", ctypes.c_void_p),
                 ("dec", ctypes.c_void_p), ("pa", ctypes.c_void_p),
                 ("tod_a", ctypes.c_void_p), ("tod_b", ctypes.c_void_p)]
@@ -100,6 +103,7 @@ SIGNATURES = [
     ("pisco_set_scan", _S, [_P, _L, _P, _P, _P, _I]),
     ("pisco_set_scan_device", _S, [_P, _L, _P, _P, _P, _P]),
     ("pisco_set_interp", _S, [_P, _I]),
+    ("pisco_set_sample_order", _S, [_P, _I]),
     ("pisco_forward", _S, [_P, ctypes.c_char, _P, _P, _I, _I]),
     ("pisco_forward_device", _S, [_P, _I, _L, _L, _P, _P, _I, _P]),
     ("pisco_sync", _S, [_P]),

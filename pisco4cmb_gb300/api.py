@@ -263,6 +263,14 @@ class GPUConvolver:
     def set_interp(self, bilinear: bool) -> None:
         check(load().pisco_set_interp(self.ctx, 1 if bilinear else 0), self.ctx, "set_interp")
 
+    def set_sample_order(self, order: str) -> None:
+        """"scan" (default) or "sky": process each launch's samples sorted by
+        sky cell (TOD identical, written in scan order)."""
+        if order not in ("scan", "sky"):
+            raise PiscoInvalidArgument(1, "order must be 'scan' or 'sky'")
+        check(load().pisco_set_sample_order(self.ctx, 1 if order == "sky" else 0), self.ctx,
+              "set_sample_order")
+
     def exec_convolution(self, data_a: np.ndarray, data_b: np.ndarray, polFlag: str = "p",
                          form: str | None = None) -> None:
         """Fill data_a/data_b (float32 or float64 arrays of nsamples) in place."""
@@ -343,12 +351,14 @@ class GPUConvolver:
               self.ctx, "set_beam_slot")
 
     @staticmethod
-    def det_descs(dets) -> ctypes.Array:
-        """dets: iterable of (slot, n, d_ra, d_dec, d_pa, d_tod_a, d_tod_b)."""
+    def det_descs(dets, sky_order: bool = False) -> ctypes.Array:
+        """dets: iterable of (slot, n, d_ra, d_dec, d_pa, d_tod_a, d_tod_b);
+        sky_order: process every pair's samples in sky order."""
         dets = list(dets)
         arr = (_lib.DetDesc * len(dets))()
+        flags = _lib.PISCO_DET_SKY_ORDER if sky_order else 0
         for i, (slot, n, ra, dec, pa, ta, tb) in enumerate(dets):
-            arr[i] = _lib.DetDesc(int(slot), 0, int(n), ra, dec, pa, ta or None, tb or None)
+            arr[i] = _lib.DetDesc(int(slot), flags, int(n), ra, dec, pa, ta or None, tb or None)
         return arr
 
     def forward_batched(self, descs, out_f64: bool = False, chunk: int = 0, stream: int = 0) -> None:

@@ -150,14 +150,15 @@ __global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(Adj
     tuned::Queue Q{0, 0};
     const tuned::Out none{nullptr, nullptr, 0, 0};
     for (long long i = gw; i < a.n; i += nw) {
-        const long long s = a.begin + i;
-        const double ga = a.g_f64 ? ((const double*)a.g_a)[i] : (double)((const float*)a.g_a)[i];
-        const double gb = a.g_f64 ? ((const double*)a.g_b)[i] : (double)((const float*)a.g_b)[i];
+        const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i
+        const long long s = a.begin + j;
+        const double ga = a.g_f64 ? ((const double*)a.g_a)[j] : (double)((const float*)a.g_a)[j];
+        const double gb = a.g_f64 ? ((const double*)a.g_b)[j] : (double)((const float*)a.g_b)[j];
         if (ga == 0.0 && gb == 0.0) continue;
         act.ga = (float)ga;
         act.gb = (float)gb;
-        tuned::sample<false>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], none, S, Q, lane, a.err, act,
-                             nfall, cmax, npairs);
+        tuned::sample<false>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], none, S, Q, lane,
+                             a.err, act, nfall, cmax, npairs);
     }
     tuned::flush(hs, S, Q, lane, a.err, act);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);

@@ -63,8 +63,14 @@ pisco_ctx::~pisco_ctx()
     for (auto& s : slots)
         if (s.beam) cudaFree(s.beam);
     for (void* p : {(void*)d_dets, (void*)d_items, (void*)d_queue, (void*)adj_sky32,
-                    (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red})
+                    (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red,
+                    (void*)rings, (void*)ord, (void*)ord_keys, (void*)ord_keys2,
+                    (void*)ord_pos, ord_tmp})
         if (p) cudaFree(p);
+    for (int* p : det_ord)
+        if (p) cudaFree(p);
+    if (ord_event) cudaEventDestroy(ord_event);
+    if (batch_event) cudaEventDestroy(batch_event);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -95,6 +101,63 @@ pisco_status pisco_ctx::ensure(void** p, size_t* cap, size_t bytes, const char* 
     *cap = bytes;
     mem_used += bytes;
     return PISCO_OK;
+}
+
+pisco_status pisco_ctx::ensure_rings(cudaStream_t s)
+{
+    pisco_ctx* c = this;
+    if (rings && rings_nside == nside_sky) return PISCO_OK;
+    pisco_status st = ensure((void**)&rings, &rings_cap, sizeof(pisco::RingT) * pisco::kMaxRings,
+                             "ring table");
+    if (st != PISCO_OK) return st;
+    CK(pisco::launch_ring_table(nside_sky, rings, s), "ring table");
+    rings_nside = nside_sky;
+    return PISCO_OK;
+}
+
+pisco_status pisco_ctx::make_order(const double* pra, const double* pdec, long long n, int** buf,
+                                   size_t* cap, cudaStream_t s)
+{
+    pisco_ctx* c = this;
+    size_t tmp_bytes = 0;
+    CK(pisco::sky_order(n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &tmp_bytes,
+                        s),
+       "sky order size");
+    const size_t nb = sizeof(int) * (size_t)n;
+    pisco_status st = ensure((void**)&ord_keys, &ord_keys_cap, nb, "order keys");
+    if (st == PISCO_OK) st = ensure((void**)&ord_keys2, &ord_keys2_cap, nb, "order keys");
+    if (st == PISCO_OK) st = ensure((void**)&ord_pos, &ord_pos_cap, nb, "order positions");
+    if (st == PISCO_OK) st = ensure(&ord_tmp, &ord_tmp_cap, tmp_bytes > 0 ? tmp_bytes : 16, "order sort");
+    if (st == PISCO_OK) st = ensure((void**)buf, cap, nb, "sample order");
+    if (st != PISCO_OK) return st;
+    tmp_bytes = ord_tmp_cap;
+    CK(pisco::sky_order(n, pra, pdec, ord_keys, ord_keys2, ord_pos, *buf, ord_tmp, &tmp_bytes, s),
+       "sky order");
+    return PISCO_OK;
+}
+
+pisco_status pisco_ctx::range_order(long long begin, long long n, cudaStream_t s, const int** out)
+{
+    pisco_ctx* c = this;
+    *out = nullptr;
+    if (sample_order != PISCO_ORDER_SKY || n < 2 || n > 0x7fffffffLL) return PISCO_OK;
+    if (!ord_event) CK(cudaEventCreateWithFlags(&ord_event, cudaEventDisableTiming), "order event");
+    else CK(cudaStreamWaitEvent(s, ord_event, 0), "order wait");
+    if (!(ord && ord_begin == begin && ord_n == n && ord_version == scan_version)) {
+        ord_n = -1;
+        pisco_status st = make_order(ra + begin, dec + begin, n, &ord, &ord_cap, s);
+        if (st != PISCO_OK) return st;
+        ord_begin = begin;
+        ord_n = n;
+        ord_version = scan_version;
+    }
+    *out = ord;
+    return PISCO_OK;
+}
+
+void pisco_ctx::order_used(cudaStream_t s)
+{
+    if (ord_event) cudaEventRecord(ord_event, s);
 }
 
 pisco_status pisco_ctx::check_device()
@@ -223,6 +286,15 @@ pisco_status pisco_set_interp(pisco_ctx* c, pisco_interp interp)
     return PISCO_OK;
 }
 
+pisco_status pisco_set_sample_order(pisco_ctx* c, pisco_order order)
+{
+    if (!c) return PISCO_ERR_INVALID_ARGUMENT;
+    if (order != PISCO_ORDER_SCAN && order != PISCO_ORDER_SKY)
+        return fail(c, PISCO_ERR_INVALID_ARGUMENT, "order must be SCAN or SKY");
+    c->sample_order = order;
+    return PISCO_OK;
+}
+
 static bool valid_nside(int nside) { return nside >= 1 && nside <= 8192; }
 
 pisco_status pisco_set_sky(pisco_ctx* c, int nside, const void* I, const void* Q, const void* U,
@@ -275,9 +347,11 @@ pisco_status pisco_set_sky(pisco_ctx* c, int nside, const void* I, const void* Q
            "sky64 H2D");
         c->sky64_valid = true;
     }
-    CK(cudaStreamSynchronize(c->stream), "sky upload");
     c->nside_sky = nside;
     c->pairs_valid = false;
+    st = c->ensure_rings(c->stream);
+    if (st != PISCO_OK) return st;
+    CK(cudaStreamSynchronize(c->stream), "sky upload");
     return PISCO_OK;
 }
 
@@ -305,6 +379,10 @@ pisco_status pisco_set_sky_device(pisco_ctx* c, int nside, const void* d_iquv, p
     } else {
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
     }
+    c->nside_sky = nside;
+    c->pairs_valid = false;
+    st = c->ensure_rings(s);
+    if (st != PISCO_OK) return st;
     if (s != c->stream) {
         cudaEvent_t ev;
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
@@ -312,8 +390,6 @@ pisco_status pisco_set_sky_device(pisco_ctx* c, int nside, const void* d_iquv, p
         cudaStreamWaitEvent(c->stream, ev, 0);
         cudaEventDestroy(ev);
     }
-    c->nside_sky = nside;
-    c->pairs_valid = false;
     return PISCO_OK;
 }
 
@@ -410,6 +486,7 @@ pisco_status pisco_set_scan(pisco_ctx* c, long n, const void* ra, const void* de
     CK(cudaStreamSynchronize(c->stream), "scan upload");
     c->nsamples = n;
     c->pairs_valid = false;
+    ++c->scan_version;
     return PISCO_OK;
 }
 
@@ -441,6 +518,7 @@ pisco_status pisco_set_scan_device(pisco_ctx* c, long n, const double* d_ra, con
     }
     c->nsamples = n;
     c->pairs_valid = false;
+    ++c->scan_version;
     return PISCO_OK;
 }
 
@@ -460,9 +538,10 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
     pisco_status st = c->activate();
     if (st != PISCO_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-    FwdArgs a;
+    FwdArgs a{};
     a.nside_sky = c->nside_sky;
     a.sky32 = c->sky32;
+    a.rings = c->rings;
     a.sky64 = nullptr;
     a.nside_beam = c->nside_beam;
     a.npix_beam = (int)c->npix_beam;
@@ -476,6 +555,8 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
     a.pa = c->pa;
     a.out_a = d_a;
     a.out_b = d_b;
+    st = c->range_order(begin, n, s, &a.order);
+    if (st != PISCO_OK) return st;
     a.out_f64 = out_dtype == PISCO_FLOAT64;
     a.interp = (int)c->interp;
     a.err = c->d_err;
@@ -507,6 +588,7 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
         // lookup or a beam reaching beyond the polar cap of its grid).
         e = launch_forward_plain(a, false, c->sm_count, s);
     }
+    if (a.order) c->order_used(s);
     if (e != cudaSuccess) return cuda_fail(c, e, "forward launch");
     if (s != c->stream) {
         cudaEvent_t ev;
@@ -612,6 +694,7 @@ pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* wor
     FwdArgs a{};
     a.nside_sky = c->nside_sky;
     a.sky32 = c->sky32;
+    a.rings = c->rings;
     a.nside_beam = c->nside_beam;
     a.npix_beam = (int)c->npix_beam;
     a.beam32 = c->beam32;

@@ -131,6 +131,7 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     AdjArgs a{};
     a.nside_sky = c->nside_sky;
     a.sky32 = c->sky32;
+    a.rings = c->rings;
     a.nside_beam = c->nside_beam;
     a.npix_beam = (int)c->npix_beam;
     a.beam32 = c->beam32;
@@ -143,6 +144,8 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     a.g_a = d_ga;
     a.g_b = d_gb;
     a.g_f64 = g_dtype == PISCO_FLOAT64;
+    st = c->range_order(begin, n, s, &a.order);
+    if (st != PISCO_OK) return st;
     a.err = c->d_err;
     a.fallbacks = c->d_fallbacks;
     CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
@@ -171,6 +174,7 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
         a.gsky32 = gs;
         a.gbeam32 = gbm;
         if (n > 0) CK(launch_adjoint(a, c->sm_count, s), "adjoint launch");
+        if (a.order) c->order_used(s);
         if (d_gsky && out_dtype == PISCO_FLOAT64) {
             widen_f32<<<1024, 256, 0, s>>>(gs, (double*)d_gsky, nsky);
             CK(cudaGetLastError(), "widen sky gradient");
@@ -212,7 +216,9 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
             CK(cudaMemsetAsync(c->adj_beam_fx, 0, 8 * nbeam, s), "zero beam accumulator");
             a.gbeam_fx = c->adj_beam_fx;
         }
-        if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0)) CK(launch_adjoint(a, c->sm_count, s), "adjoint launch");
+        if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0))
+            CK(launch_adjoint(a, c->sm_count, s), "adjoint launch");
+        if (a.order) c->order_used(s);
         if (d_gsky)
             CK(launch_fixed_to_float(c->adj_sky_fx, d_gsky, out_dtype == PISCO_FLOAT64, nsky,
                                      a.sky_scale > 0.0 ? 1.0 / a.sky_scale : 0.0, s),

@@ -64,6 +64,8 @@ pisco_status validate(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_
             return fail(c, PISCO_ERR_INVALID_ARGUMENT, "detector " + std::to_string(d) + ": bad nsamples");
         if (x.nsamples > 0 && (!x.ra || !x.dec || !x.pa))
             return fail(c, PISCO_ERR_INVALID_ARGUMENT, "detector " + std::to_string(d) + ": NULL pointing");
+        if (x.flags & ~PISCO_DET_SKY_ORDER)
+            return fail(c, PISCO_ERR_INVALID_ARGUMENT, "detector " + std::to_string(d) + ": unknown flags");
         const auto& s = c->slots[x.beam_slot];
         if (!tuned_supported(s.nside, (int)s.npix, s.rho_max))
             return fail(c, PISCO_ERR_UNSUPPORTED,
@@ -176,13 +178,29 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     const std::string key = launch_key(c, dets, ndet, out_dtype, chunk);
     if (!(c->graph_exec && key == c->graph_key)) {
+        // the descriptors, items and orders below may still be read by the
+        // previous launch (on another stream)
+        if (c->batch_event) CK(cudaStreamWaitEvent(c->stream, c->batch_event, 0), "batch wait");
         std::vector<BatchDet> bd(ndet);
         std::vector<double> cost(ndet);
+        if ((int)c->det_ord.size() < ndet) {
+            c->det_ord.resize(ndet, nullptr);
+            c->det_ord_cap.resize(ndet, 0);
+        }
         for (int d = 0; d < ndet; ++d) {
             const auto& sl = c->slots[dets[d].beam_slot];
+            const int* order = nullptr;
+            if ((dets[d].flags & PISCO_DET_SKY_ORDER) && dets[d].nsamples >= 2 &&
+                dets[d].nsamples <= 0x7fffffffLL) {
+                st = c->make_order(dets[d].ra, dets[d].dec, dets[d].nsamples, &c->det_ord[d],
+                                   &c->det_ord_cap[d], c->stream);
+                if (st != PISCO_OK) return st;
+                order = c->det_ord[d];
+            }
             bd[d] = BatchDet{sl.beam, sl.nside, (int)sl.npix, sl.rho_max,
                              (float)(1.7320508075688772 * sl.nside), dets[d].nsamples,
-                             dets[d].ra, dets[d].dec, dets[d].pa, dets[d].tod_a, dets[d].tod_b};
+                             dets[d].ra, dets[d].dec, dets[d].pa, dets[d].tod_a, dets[d].tod_b,
+                             order};
             cost[d] = disc_pairs(c->nside_sky, sl.rho_max);
         }
         const std::vector<BatchItem> items = make_items(bd, cost, chunk);
@@ -204,6 +222,7 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         BatchArgs a;
         a.nside_sky = c->nside_sky;
         a.sky32 = c->sky32;
+        a.rings = c->rings;
         a.dets = c->d_dets;
         a.ndet = ndet;
         a.items = c->d_items;
@@ -236,6 +255,8 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         c->graph_key = key;
     }
     CK(cudaGraphLaunch(c->graph_exec, s), "graph launch");
+    if (!c->batch_event) CK(cudaEventCreateWithFlags(&c->batch_event, cudaEventDisableTiming), "event");
+    CK(cudaEventRecord(c->batch_event, s), "batch event");
     return PISCO_OK;
 }
 

@@ -29,6 +29,11 @@ struct pisco_ctx {
     pisco::D4* sky64 = nullptr;
     size_t sky64_cap = 0;
     bool sky64_valid = false;
+    // ring table of the sky grid (allocated once for the largest nside, so
+    // its address never changes; rebuilt when nside changes)
+    pisco::RingT* rings = nullptr;
+    size_t rings_cap = 0;
+    int rings_nside = 0;
 
     // beam (partial RING map around the north pole, a|b interleaved)
     int nside_beam = 0;
@@ -47,6 +52,26 @@ struct pisco_ctx {
     double* dec = nullptr;
     double* pa = nullptr;
     size_t ra_cap = 0, dec_cap = 0, pa_cap = 0;
+
+    // sample order (pisco_set_sample_order): the sky order of the last
+    // forward/adjoint range, cached until the scan or the range changes
+    int sample_order = 0;  // pisco_order
+    long long scan_version = 0;
+    int* ord = nullptr;
+    size_t ord_cap = 0;
+    long long ord_begin = -1, ord_n = -1, ord_version = -1;
+    cudaEvent_t ord_event = nullptr;  // recorded after the last write or read of ord
+    unsigned* ord_keys = nullptr;
+    size_t ord_keys_cap = 0;
+    unsigned* ord_keys2 = nullptr;
+    size_t ord_keys2_cap = 0;
+    int* ord_pos = nullptr;
+    size_t ord_pos_cap = 0;
+    void* ord_tmp = nullptr;
+    size_t ord_tmp_cap = 0;
+    std::vector<int*> det_ord;  // batched: per-descriptor orders
+    std::vector<size_t> det_ord_cap;
+    cudaEvent_t batch_event = nullptr;  // recorded after the last batched launch
 
     // staging and bookkeeping
     void* out_dev = nullptr;
@@ -91,5 +116,16 @@ struct pisco_ctx {
     ~pisco_ctx();
     pisco_status activate();
     pisco_status ensure(void** p, size_t* cap, size_t bytes, const char* what);
+    // ring table for nside_sky, built on stream s if nside changed
+    pisco_status ensure_rings(cudaStream_t s);
+    // sky order of n pointings into *buf (n ints, grown as needed), on s
+    pisco_status make_order(const double* ra, const double* dec, long long n, int** buf,
+                            size_t* cap, cudaStream_t s);
+    // order of samples [begin, begin + n) of the scan for a launch on s:
+    // null in scan order (or n < 2 or n >= 2^31), else the cached or new
+    // sky order.  Stream s first waits for the previous access to the order
+    // buffer; a launch that reads it calls order_used(s) afterwards.
+    pisco_status range_order(long long begin, long long n, cudaStream_t s, const int** out);
+    void order_used(cudaStream_t s);
     pisco_status check_device();
 };

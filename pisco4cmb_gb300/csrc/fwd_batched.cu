@@ -40,10 +40,24 @@ constexpr int kBW = 8;  // warps per block
 // A block pulls one item at a time and its warps take the item's samples
 // round-robin, so the warps of an SM work on neighbouring samples (whose
 // discs overlap) at the same moment, as in the single-detector launch.
+// The block's current item, set up once by thread 0.
+struct ItemState {
+    Hpx hb;
+    tuned::Beam B;
+    const double* ra;
+    const double* dec;
+    const double* pa;
+    void* out_a;
+    void* out_b;
+    const int* order;  // position -> sample, or null
+    long long begin, end;
+    int state;  // 0: queue empty, 1: run, 2: bad item (skipped)
+};
+
 __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(BatchArgs a)
 {
     __shared__ tuned::WarpSmem sm[kBW];
-    __shared__ int s_item[2];
+    __shared__ ItemState s_item[2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     tuned::WarpSmem& S = sm[warp];
@@ -55,23 +69,41 @@ __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(Bat
     tuned::Queue Q{0, 0};
     for (int round = 0;; ++round) {
         // double-buffered: a slot is rewritten only after the next barrier,
-        // which every thread reaches after reading it
-        if (threadIdx.x == 0) s_item[round & 1] = (int)atomicAdd(a.queue, 1u);
-        __syncthreads();
-        const int item = s_item[round & 1];
-        if (item >= a.nitems) break;
-        const BatchItem it = a.items[item];
-        if (it.det < 0 || it.det >= a.ndet) {
-            if (threadIdx.x == 0) tuned::record(a.err, kCheckQueue);
-            continue;
+        // which every thread reaches after it is done with the slot
+        ItemState& T = s_item[round & 1];
+        if (threadIdx.x == 0) {
+            const int item = (int)atomicAdd(a.queue, 1u);
+            T.state = 0;
+            if (item < a.nitems) {
+                const BatchItem it = a.items[item];
+                if (it.det < 0 || it.det >= a.ndet) {
+                    tuned::record(a.err, kCheckQueue);
+                    T.state = 2;
+                } else {
+                    const BatchDet& d = a.dets[it.det];
+                    T.hb = hpx_make(d.nside_beam);
+                    T.B = tuned::make_beam(d.beam, d.nside_beam, d.npix_beam, d.rho_max);
+                    T.ra = d.ra;
+                    T.dec = d.dec;
+                    T.pa = d.pa;
+                    T.out_a = d.out_a;
+                    T.out_b = d.out_b;
+                    T.order = d.order;
+                    T.begin = it.begin;
+                    T.end = it.begin + it.count;
+                    T.state = 1;
+                }
+            }
         }
-        const BatchDet d = a.dets[it.det];
-        const Hpx hb = hpx_make(d.nside_beam);
-        const tuned::Beam B = tuned::make_beam(d.beam, d.nside_beam, d.npix_beam, d.rho_max);
-        for (long long s = it.begin + warp; s < it.begin + it.count; s += kBW) {
-            const tuned::Out o{d.out_a, d.out_b, s, a.out_f64};
-            tuned::sample<false>(hs, hb, B, d.ra[s], d.dec[s], d.pa[s], o, S, Q, lane, a.err, g,
-                                 nfall, cmax, npairs);
+        __syncthreads();
+        const int state = T.state;
+        if (state == 0) break;
+        if (state == 2) continue;
+        for (long long p = T.begin + warp; p < T.end; p += kBW) {
+            const long long s = T.order ? (long long)T.order[p] : p;  // sample of position p
+            const tuned::Out o{T.out_a, T.out_b, s, a.out_f64};
+            tuned::sample<false>(hs, a.rings, T.hb, T.B, T.ra[s], T.dec[s], T.pa[s], o, S, Q, lane,
+                                 a.err, g, nfall, cmax, npairs);
         }
     }
     tuned::flush(hs, S, Q, lane, a.err, g);

@@ -171,17 +171,18 @@ __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
     const long long gw = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kWarps;
     for (long long i = gw; i < a.n; i += nw) {
-        const long long s = a.begin + i;
+        const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i
+        const long long s = a.begin + j;
         const double ra = a.ra[s], dec = a.dec[s], psi = -a.pa[s];
         if (!(isfinite(ra) && isfinite(dec) && isfinite(psi))) {
             // non-finite pointing: NaN out (never let it reach the ring loop bounds)
             if (lane == 0) {
                 if (a.out_f64) {
-                    if (a.out_a) ((double*)a.out_a)[i] = CUDART_NAN;
-                    if (a.out_b) ((double*)a.out_b)[i] = CUDART_NAN;
+                    if (a.out_a) ((double*)a.out_a)[j] = CUDART_NAN;
+                    if (a.out_b) ((double*)a.out_b)[j] = CUDART_NAN;
                 } else {
-                    if (a.out_a) ((float*)a.out_a)[i] = CUDART_NAN_F;
-                    if (a.out_b) ((float*)a.out_b)[i] = CUDART_NAN_F;
+                    if (a.out_a) ((float*)a.out_a)[j] = CUDART_NAN_F;
+                    if (a.out_b) ((float*)a.out_b)[j] = CUDART_NAN_F;
                 }
             }
             continue;
@@ -223,11 +224,11 @@ __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
         }
         if (lane == 0) {
             if (a.out_f64) {
-                if (a.out_a) ((double*)a.out_a)[i] = acc_a;
-                if (a.out_b) ((double*)a.out_b)[i] = acc_b;
+                if (a.out_a) ((double*)a.out_a)[j] = acc_a;
+                if (a.out_b) ((double*)a.out_b)[j] = acc_b;
             } else {
-                if (a.out_a) ((float*)a.out_a)[i] = (float)acc_a;
-                if (a.out_b) ((float*)a.out_b)[i] = (float)acc_b;
+                if (a.out_a) ((float*)a.out_a)[j] = (float)acc_a;
+                if (a.out_b) ((float*)a.out_b)[j] = (float)acc_b;
             }
         }
     }

@@ -35,10 +35,11 @@ __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
     g.sky = a.sky32;
     tuned::Queue Q{0, 0};
     for (long long i = gw; i < a.n; i += nw) {
-        const long long s = a.begin + i;
-        const tuned::Out o{a.out_a, a.out_b, i, a.out_f64};
-        tuned::sample<kCalib>(hs, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane, a.err, g, nfall,
-                              cmax, npairs);
+        const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i
+        const long long s = a.begin + j;
+        const tuned::Out o{a.out_a, a.out_b, j, a.out_f64};
+        tuned::sample<kCalib>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane, a.err,
+                              g, nfall, cmax, npairs);
     }
     tuned::flush(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
@@ -49,6 +50,30 @@ __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
             atomicMax((int*)calib, __float_as_int(cmax));
             atomicAdd(reinterpret_cast<unsigned long long*>(calib + 2), npairs);
         }
+    }
+}
+
+__global__ void ring_table_kernel(int nside, RingT* rings)
+{
+    const Hpx h = hpx_make(nside);
+    const long long nr = 4LL * nside - 1;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x + 1; r <= nr;
+         r += (long long)gridDim.x * blockDim.x) {
+        const RingInfo ri = ring_info(h, r);
+        const double z = ring2z(h, r);
+        const double s = sqrt(PD_MUL(PD_SUB(1.0, z), PD_ADD(1.0, z)));
+        RingT t;
+        t.z = z;
+        t.omz2 = PD_SUB(1.0, PD_MUL(z, z));
+        t.dec = atan2(z, s);
+        t.fr = PD_MUL((double)ri.npix, kInvTwoPi);
+        t.dphi = PD_DIV(kTwoPi, (double)ri.npix);
+        t.s = (float)s;
+        t.dphif = (float)t.dphi;
+        t.zf = (float)z;
+        t.start = (int)ri.start;
+        t.npix2 = (int)(2 * ri.npix + (ri.shifted ? 1 : 0));
+        rings[r - 1] = t;
     }
 }
 
@@ -89,6 +114,14 @@ bool tuned_supported(int nside_beam, int npix_beam, double rho_max)
     if (ring + 2.0 >= nside_beam) return false;
     const long long ncap = 2LL * nside_beam * (nside_beam - 1);
     return npix_beam <= ncap;
+}
+
+cudaError_t launch_ring_table(int nside, RingT* rings, cudaStream_t st)
+{
+    if (nside < 1 || nside > 8192 || !rings) return cudaErrorInvalidValue;
+    const long long nr = 4LL * nside - 1;
+    ring_table_kernel<<<(int)((nr + 255) / 256), 256, 0, st>>>(nside, rings);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st)

@@ -307,6 +307,8 @@ PHD void get_interpol(const Hpx& h, double theta, double phi, int64_t pix[4], do
 // ---------------------------------------------------------------------------
 struct DiscPlan {
     double z0, xa, cosr, phi;
+    double theta, s0;  // normalised colatitude in [0, pi] and sqrt((1 - z0)(1 + z0))
+    bool flip;         // the centre was reflected (colatitude beyond pi, phi + pi)
     int64_t ring_lo, ring_hi;  // rings evaluated with the edge formula
     int64_t full_lo, full_hi;  // first and last ring touched at all
     bool all_sky;
@@ -325,10 +327,12 @@ PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius, do
 {
     DiscPlan p;
     theta = fmodulo(theta, kTwoPi);
-    if (theta > kPi) {
+    p.flip = theta > kPi;
+    if (p.flip) {
         phi = PD_ADD(phi, kPi);
         theta = PD_SUB(kTwoPi, theta);
     }
+    p.theta = theta;
     p.phi = fmodulo(phi, kTwoPi);
     p.all_sky = radius >= kPi;
     if (p.all_sky) {
@@ -336,12 +340,13 @@ PHD DiscPlan disc_plan(const Hpx& h, double theta, double phi, double radius, do
         p.ring_hi = 0;
         p.full_lo = 1;
         p.full_hi = 4 * h.nside - 1;
-        p.z0 = p.xa = p.cosr = 0.0;
+        p.z0 = p.xa = p.cosr = p.s0 = 0.0;
         return p;
     }
     p.cosr = cosr;
     p.z0 = cos(theta);
-    p.xa = PD_DIV(1.0, sqrt(PD_MUL(PD_SUB(1.0, p.z0), PD_ADD(1.0, p.z0))));
+    p.s0 = sqrt(PD_MUL(PD_SUB(1.0, p.z0), PD_ADD(1.0, p.z0)));
+    p.xa = PD_DIV(1.0, p.s0);
     double rlat1 = PD_SUB(theta, radius);
     p.ring_lo = ring_above(h, cos(rlat1)) + 1;
     p.full_lo = (rlat1 <= 0.0 && p.ring_lo > 1) ? 1 : p.ring_lo;

@@ -25,6 +25,25 @@ struct alignas(64) D8 {
     D4 a, b;
 };
 
+// Per-ring geometry of the sky grid, built once per nside on the device
+// (ring_table_kernel, fwd_tuned.cu) from hpx.cuh's ring_info and ring2z, so
+// every value is the one the HEALPix formulas give: rings 1 .. 4 nside - 1
+// at index ring - 1.  64 bytes, four 16-byte loads.  At most 32,767 rings
+// (nside 8192): 2.1 MB.
+struct alignas(16) RingT {
+    double z;      // ring2z
+    double omz2;   // 1 - z*z, rounded as the disc-edge formula rounds it
+    double dec;    // latitude atan2(z, sqrt((1 - z)(1 + z)))
+    double fr;     // npix / (2 pi), rounded as the disc-edge formula rounds it
+    double dphi;   // 2 pi / npix
+    float s;       // sqrt(1 - z^2)
+    float dphif;   // 2 pi / npix
+    float zf;      // z
+    int start;     // first pixel
+    int npix2;     // 2 npix + (1 if the ring is shifted by half a pixel)
+};
+constexpr int kMaxRings = 4 * 8192 - 1;
+
 // Device-side check codes written to the context's error word (first one
 // wins).  Kernels never trap: they record the code, skip the access and
 // finish.
@@ -39,6 +58,7 @@ enum DevCheck : unsigned int {
 
 struct FwdArgs {
     int nside_sky;
+    const RingT* rings;  // sky ring table (TUNED form)
     const float4* sky32;
     const D4* sky64;
     int nside_beam;
@@ -52,6 +72,7 @@ struct FwdArgs {
     const double* pa;
     void* out_a;  // may be null
     void* out_b;  // may be null
+    const int* order;  // position -> sample (sky order) or null (scan order)
     int out_f64;
     int interp;  // 0 nearest, 1 bilinear
     unsigned int* err;
@@ -71,6 +92,7 @@ struct BatchDet {
     const double* pa;
     void* out_a;
     void* out_b;
+    const int* order;  // position -> sample (sky order) or null
 };
 
 // One unit of the work queue: samples [begin, begin + count) of detector det.
@@ -82,6 +104,7 @@ struct BatchItem {
 
 struct BatchArgs {
     int nside_sky;
+    const RingT* rings;  // sky ring table
     const float4* sky32;
     const BatchDet* dets;
     int ndet;
@@ -95,6 +118,7 @@ struct BatchArgs {
 
 struct AdjArgs {
     int nside_sky;
+    const RingT* rings;  // sky ring table
     const float4* sky32;  // needed for the beam gradient
     int nside_beam;
     int npix_beam;
@@ -106,6 +130,7 @@ struct AdjArgs {
     const double* pa;
     const void* g_a;  // dL/dTOD a, b (n values each)
     const void* g_b;
+    const int* order;  // position -> sample (sky order) or null
     int g_f64;
     int fixed;                     // 1: fixed-point int64 accumulation
     float* gsky32;                 // atomic: [npix][4] or null
@@ -133,6 +158,15 @@ bool tuned_supported(int nside_beam, int npix_beam, double rho_max);
 // Same kernel with every FP32 decision also evaluated in FP64: writes the
 // worst |FP32 - FP64| / margin seen over the non-fallback pairs to *calib.
 cudaError_t launch_tuned_calibrate(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib);
+// Sky order of n < 2^31 samples (order.cu).  With tmp == NULL stores the
+// temporary bytes the sort needs in *tmp_bytes and does nothing else;
+// otherwise writes order[0..n): the positions 0..n-1 sorted by the Z-order
+// code of their pointing's sky cell (keys, keys_sorted, pos: n each).
+cudaError_t sky_order(long long n, const double* ra, const double* dec, unsigned* keys,
+                      unsigned* keys_sorted, int* pos, int* order, void* tmp, size_t* tmp_bytes,
+                      cudaStream_t st);
+// Fills the sky ring table (4 nside - 1 entries) for nside <= 8192.
+cudaError_t launch_ring_table(int nside, RingT* rings, cudaStream_t st);
 // Batched TUNED forward (fwd_batched.cu).
 int batched_grid(int sm_count);
 cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st);

@@ -12,8 +12,9 @@
 // library.
 //
 // The working memory is g_noalloc_scratch below: a file-scope
-// static __device__ array of kScratchBytes (about 0.5 MB).  Every GPU that
-// loads the library holds it until the process exits.  It holds the
+// static __device__ array of kScratchBytes (about 2.6 MB).  Every GPU that
+// loads the library holds it until the process exits.  It holds the sky
+// ring table (2.1 MB, sized for nside 8192), the
 // detector descriptors (at most PISCO_NOALLOC_MAX_DETS), the work items (at
 // most PISCO_NOALLOC_MAX_ITEMS), the queue counter, the device error word
 // and the FP64-fallback counter.  All calls share it and it keeps the last
@@ -48,6 +49,7 @@ constexpr int kMaxItems = PISCO_NOALLOC_MAX_ITEMS;
 constexpr int kMaxDevices = 64;
 
 struct Scratch {
+    RingT rings[kMaxRings];  // sky ring table, rebuilt by every call
     BatchDet dets[kMaxDets];
     BatchItem items[kMaxItems];
     unsigned int queue;
@@ -178,8 +180,11 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
     }
     cudaStream_t st = (cudaStream_t)stream;
     noalloc_setup_kernel<<<1, 256, 0, st>>>(p, scratch);
+    cudaError_t e0 = cudaGetLastError();
+    if (e0 == cudaSuccess) e0 = launch_ring_table(nside_sky, scratch->rings, st);
     BatchArgs a;
     a.nside_sky = nside_sky;
+    a.rings = scratch->rings;
     a.sky32 = (const float4*)d_sky_iquv;
     a.dets = scratch->dets;
     a.ndet = ndet;
@@ -189,7 +194,7 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
     a.out_f64 = 0;
     a.err = &scratch->err;
     a.fallbacks = &scratch->fallbacks;
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = e0;
     if (e == cudaSuccess) e = launch_batched(a, batched_grid(sms), st);
     // synchronous: read the device error word back
     unsigned int code = 0;

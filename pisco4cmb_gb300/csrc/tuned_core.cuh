@@ -199,21 +199,22 @@ __device__ __forceinline__ float rcp_approx(float x)
 // exact FP64 HEALPix formula (disc_ring) whenever an edge decision is within
 // the FP32 angle's error of a pixel boundary.  Same result as disc_ring.
 __device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan& p, long long ring,
-                                                   double z, const RingInfo& ri)
+                                                   const RingT& rt)
 {
     RingSpan s = {0, 0, 0, 0};
     if (ring < p.full_lo || ring > p.full_hi) return s;
+    const long long npix = rt.npix2 >> 1;
     if (p.all_sky || ring < p.ring_lo || ring > p.ring_hi) {
-        s.start1 = ri.start;
-        s.n1 = ri.npix;
+        s.start1 = rt.start;
+        s.n1 = npix;
         return s;
     }
-    const double x = PD_MUL(PD_SUB(p.cosr, PD_MUL(z, p.z0)), p.xa);
-    const double ysq = PD_SUB(PD_SUB(1.0, PD_MUL(z, z)), PD_MUL(x, x));
+    const double x = PD_MUL(PD_SUB(p.cosr, PD_MUL(rt.z, p.z0)), p.xa);
+    const double ysq = PD_SUB(rt.omz2, PD_MUL(x, x));
     if (!(ysq > 0.0)) return s;  // no intersection (HEALPix: dphi = 0, ring skipped)
     const float de = atan2f(sqrtf((float)ysq), (float)x);
-    const double shift = ri.shifted ? 0.5 : 0.0;
-    const double fr = (double)ri.npix * kInvTwoPi;
+    const double shift = (rt.npix2 & 1) ? 0.5 : 0.0;
+    const double fr = rt.fr;
     const double vlo = fr * (p.phi - (double)de) - shift;
     const double vhi = fr * (p.phi + (double)de) - shift;
     // |de - atan2(sqrt(ysq), x)| <= 3e-7 de (FP32 rounding of x, ysq and atan2f)
@@ -224,17 +225,17 @@ __device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan&
     long long lo = (long long)floor(vlo) + 1;
     long long hi = (long long)floor(vhi);
     if (lo > hi) return s;
-    if (hi >= ri.npix) {
-        lo -= ri.npix;
-        hi -= ri.npix;
+    if (hi >= npix) {
+        lo -= npix;
+        hi -= npix;
     }
     if (lo < 0) {
-        s.start1 = ri.start;
+        s.start1 = rt.start;
         s.n1 = hi + 1;
-        s.start2 = ri.start + lo + ri.npix;
+        s.start2 = rt.start + lo + npix;
         s.n2 = -lo;
     } else {
-        s.start1 = ri.start + lo;
+        s.start1 = rt.start + lo;
         s.n1 = hi - lo + 1;
     }
     return s;
@@ -357,7 +358,8 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
 // the disc pairs (lane 0 only); cmax (kCalib) is the worst FP32 decision
 // error over the non-queued pairs, in units of the margin.
 template <bool kCalib, class Action>
-__device__ __forceinline__ void sample(const Hpx& hs, const Hpx& hb, const Beam& B, double ra,
+__device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const Hpx& hb,
+                                       const Beam& B, double ra,
                                        double dec, double pa, const Out& o, WarpSmem& S,
                                        Queue& Qs, int lane, unsigned int* err, Action& act,
                                        unsigned long long& nfall, float& cmax,
@@ -408,16 +410,31 @@ __device__ __forceinline__ void sample(const Hpx& hs, const Hpx& hb, const Beam&
     // exp(2i chi) are unchanged.  So the geometry runs in the normalised frame
     // (s0 >= 0) with (sin psi, cos psi) negated, which adds exactly pi to
     // sigma.  ra is reduced mod 2pi (the anchor longitude of the rings).
-    double sdec, cdec;
-    sincos(F.dec, &sdec, &cdec);
-    const bool flip = cdec < 0.0;
-    const double z0d = sdec, s0d = flip ? -cdec : cdec;
-    const double phi_f = fmodulo(flip ? F.ra + kPi : F.ra, kTwoPi);
+    // The frame is disc_plan's (z0 = cos(theta), s0, phi, latitude
+    // pi/2 - theta) whenever its reflection agrees with the sign of cos(dec),
+    // which decides the flip as in the reference chain; they can differ
+    // only within an ulp of the poles, where the frame is rebuilt from dec.
+    const bool flip = fabs(F.dec) < 1.5707963 ? false : cos(F.dec) < 0.0;
+    double z0d, s0d, phi_f, dec0;
+    if (flip == P.flip) {
+        z0d = P.z0;
+        s0d = P.s0;
+        phi_f = P.phi;
+        dec0 = PD_SUB(kHalfPi, P.theta);
+    } else {
+        double sdec, cdec;
+        sincos(F.dec, &sdec, &cdec);
+        z0d = sdec;
+        s0d = fabs(cdec);
+        phi_f = fmodulo(flip ? F.ra + kPi : F.ra, kTwoPi);
+        dec0 = atan2(z0d, s0d);
+    }
+    const float z0f = (float)z0d, s0f = (float)s0d;
     // psi phasors in FP64, rounded once: exp(2i psi) multiplies every pair
     // of the sample, so its rounding error is coherent over the sample sum.
     double spsi, cpsi;
     sincos(F.psi, &spsi, &cpsi);
-    F.s0 = (float)s0d;
+    F.s0 = s0f;
     F.sps = (float)(flip ? -spsi : spsi);
     F.cps = (float)(flip ? -cpsi : cpsi);
     F.c2p = (float)(cpsi * cpsi - spsi * spsi);
@@ -429,34 +446,30 @@ __device__ __forceinline__ void sample(const Hpx& hs, const Hpx& hb, const Beam&
         RingC rc;
         rc.n1 = 0;
         if (ring <= P.full_hi) {
-            const RingInfo ri = ring_info(hs, ring);
-            const double z = ring2z(hs, ring);
-            const RingSpan sp = fast_disc_ring(hs, P, ring, z, ri);
+            const RingT rt = rings[ring - 1];
+            const RingSpan sp = fast_disc_ring(hs, P, ring, rt);
             cnt = (int)(sp.n1 + sp.n2);
             if (cnt) {
-                // s = sqrt(1 - z^2) and 1/npix: FP32 seeds, one Newton step in FP64
-                const double omz = PD_MUL(PD_SUB(1.0, z), PD_ADD(1.0, z));
-                double rs = (double)rsqrtf((float)omz);
-                rs = rs * (1.5 - 0.5 * omz * rs * rs);
-                const double si = omz * rs;
-                const double nd = (double)ri.npix;
-                double rn = (double)__frcp_rn((float)ri.npix);
-                rn = rn * (2.0 - nd * rn);
-                const double dphi = kTwoPi * rn;
-                const double sh = ri.shifted ? 0.5 : 0.0;
-                const double jc = floor(phi_f * (nd * kInvTwoPi) - sh + 0.5);
-                const double dz = z - z0d, ds = si - s0d;
-                rc.dc = (float)((jc + sh) * dphi - phi_f);
-                rc.dphi = (float)dphi;
-                rc.si = (float)si;
-                rc.Di = (float)(z * s0d - si * z0d);
-                rc.Ki = (float)(0.5 * (dz * dz + ds * ds));
-                rc.Zs = (float)(si * z0d);
-                rc.Wz = (float)(s0d * z);
-                rc.Pp = (float)(si * s0d);
-                rc.nr = (int)ri.npix;
-                rc.b1 = (int)(sp.start1 - ri.start) - (int)jc;
-                rc.b2 = (int)(sp.start2 - ri.start) - (int)jc;
+                const double sh = (rt.npix2 & 1) ? 0.5 : 0.0;
+                const double jc = floor(phi_f * rt.fr - sh + 0.5);
+                rc.dc = (float)((jc + sh) * rt.dphi - phi_f);
+                rc.dphi = rt.dphif;
+                rc.si = rt.s;
+                // sin and 1 - cos of the latitude offset D: FP32 series at the
+                // rounded offset, first-order correction by its rounding error
+                const double dd = rt.dec - dec0;
+                const float df = (float)dd;
+                const float de = (float)(dd - (double)df);
+                float sD, hD;
+                sin_versin(df, sD, hD);
+                rc.Di = fmaf(de, 1.0f - hD, sD);
+                rc.Ki = fmaf(de, sD, hD);
+                rc.Zs = rt.s * z0f;
+                rc.Wz = s0f * rt.zf;
+                rc.Pp = rt.s * s0f;
+                rc.nr = rt.npix2 >> 1;
+                rc.b1 = (int)(sp.start1 - rt.start) - (int)jc;
+                rc.b2 = (int)(sp.start2 - rt.start) - (int)jc;
             }
             rc.n1 = (int)sp.n1;
             rc.s1 = (int)sp.start1;
