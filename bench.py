@@ -625,10 +625,13 @@ def run_c5_adjoint(args):
     res = {}
     for det in (True, False):
         for with_beam in (False, True):
-            key = ("deterministic" if det else "atomic") + ("_sky_and_beam" if with_beam else "_sky")
-            res[key] = timeit(lambda: conv.adjoint_device(
-                ga.data_ptr(), gb.data_ptr(), False, gsky.data_ptr(),
-                gbeam.data_ptr() if with_beam else 0, deterministic=det, stream=cs))
+            for iqu in (False, True):
+                key = (("deterministic" if det else "atomic") +
+                       ("_sky_and_beam" if with_beam else "_sky") + ("_iqu" if iqu else "_iquv"))
+                res[key] = timeit(lambda: conv.adjoint_device(
+                    ga.data_ptr(), gb.data_ptr(), False, gsky.data_ptr(),
+                    gbeam.data_ptr() if with_beam else 0, deterministic=det, stream=cs,
+                    sky_iqu=iqu))
     line = {"workload": "c5_adjoint_nside256_beam4deg", "nsamples": n, "pairs": pairs,
             "forward_ms": t_fwd * 1e3,
             "adjoint_ms": {k: v * 1e3 for k, v in res.items()},
@@ -685,6 +688,71 @@ def run_order_study(args):
     return 0
 
 
+def run_map_study(args):
+    """Binned map-making (SkyMap on the GPU): the c2 scan's two detectors (a at
+    0 deg, b at 90 deg; 4,000,000 TOD values) into an nside 1024 map: TOD
+    accumulation from device-resident FP64 pointing and TOD, and the solve.
+    CPU baseline: the map-making oracle (one thread) on a bounded prefix."""
+    import torch
+
+    import oracle
+    from pisco4cmb_gb300 import SkyMap
+
+    n = args.samples or 2_000_000
+    from pisco4cmb_gb300 import synth
+
+    ra, dec, pa = synth.sweep_scan(n, 2)
+    rng = np.random.default_rng(20261203)
+    tod = rng.normal(size=(2, n))
+    ra2, dec2, pa2 = (np.stack([x, x]) for x in (ra, dec, pa))
+    t = [torch.tensor(x.reshape(-1), device="cuda") for x in (ra2, dec2, pa2, tod)]
+    pol = np.float32([0.0, np.pi / 2])
+    cs = _study_stream()
+    m = SkyMap(1024)
+    e0, e1 = _events()
+
+    def acc():
+        m.accumulate_device(n, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 2, pol,
+                            t[3].data_ptr(), f64=True, stream=cs)
+
+    acc()  # warm-up (scratch allocation)
+    m.reset()
+    ts = []
+    for _ in range(args.steps):
+        e0.record()
+        acc()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    t_acc = float(np.median(ts)) / 1e3
+    e0.record()
+    m.solve_map()
+    e1.record()
+    torch.cuda.synchronize()
+    t_solve = e0.elapsed_time(e1) / 1e3
+    hits = m.get_hitmap()
+    # determinism: a fresh map from the same calls gives the same normal equations
+    m2 = SkyMap(1024)
+    for _ in range(args.steps):
+        m2.accumulate_device(n, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), 2, pol,
+                             t[3].data_ptr(), f64=True, stream=cs)
+    same = all(np.array_equal(x, y) for x, y in zip(m.get_normal(), m2.get_normal()))
+    # CPU: the oracle (single-threaded restatement of skymap.cpp) on a prefix
+    k = min(n, 200_000)
+    t0 = time.perf_counter()
+    oracle.map_accumulate(1024, ra2[:, :k], dec2[:, :k], pa2[:, :k], pol, tod[:, :k])
+    t_cpu = time.perf_counter() - t0
+    line = {"workload": "map_c2scan_2det_nside1024", "tod_values": 2 * n,
+            "accumulate_ms": t_acc * 1e3, "tod_values_per_s": 2 * n / t_acc,
+            "solve_ms": t_solve * 1e3, "pixels": 12 * 1024 * 1024,
+            "pixels_hit": int((hits > 0).sum()), "pixels_solved": int((hits >= 3).sum()),
+            "deterministic": same,
+            "cpu_baseline": {"tod_values_per_s": 2 * k / t_cpu, "cores": 1, "kind": "port",
+                             "sample": "first %d samples x 2 detectors" % k}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -696,7 +764,7 @@ def main():
     ap.add_argument("--accuracy-samples", type=int, default=50_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map"],
                     help="c2 = the headline line; the others print their own study lines")
     ap.add_argument("--fp64-samples", type=int, default=200_000)
     ap.add_argument("--cpu-samples", type=int, default=2_000)
@@ -714,7 +782,7 @@ def main():
         if args.samples == 2_000_000:
             args.samples = 0  # the workload's own sample count
         return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint,
-                "order": run_order_study}[args.workload](args)
+                "order": run_order_study, "map": run_map_study}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 

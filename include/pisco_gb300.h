@@ -233,7 +233,11 @@ pisco_status pisco_forward_batched_noalloc(int device, int nside_sky, const floa
  * bound on every total; bit-identical results whatever the order. */
 typedef enum pisco_adjoint_mode {
     PISCO_ADJ_ATOMIC = 0,
-    PISCO_ADJ_DETERMINISTIC = 1
+    PISCO_ADJ_DETERMINISTIC = 1,
+    /* OR-ed with either mode: the sky gradient holds I, Q, U only (its V
+     * column is written as zero and not accumulated: a quarter fewer
+     * accumulations in the DETERMINISTIC mode) */
+    PISCO_ADJ_SKY_IQU = 2
 } pisco_adjoint_mode;
 
 /* Beam from a device buffer of npix x 8 interleaved values (a.I,Q,U,V,
@@ -254,6 +258,53 @@ pisco_status pisco_adjoint_device(pisco_ctx* ctx, long begin, long n, const void
 pisco_status pisco_adjoint(pisco_ctx* ctx, const void* g_a, const void* g_b, pisco_dtype g_dtype,
                            void* gI, void* gQ, void* gU, void* gV, pisco_dtype out_dtype,
                            pisco_adjoint_mode mode);
+
+/* ---- binned map-maker (replaces SkyMap, src/SkyMap/skymap.hpp:13-56) ---
+ * Accumulates TOD into per-pixel normal equations (3 x 3 AtA and AtD, FP64,
+ * device-resident) and solves them for I, Q, U.  Each pixel's totals
+ * receive the reference's additions in the reference's order
+ * (skymap.cpp:68-132), deterministically. */
+typedef struct pisco_map pisco_map;
+/* SkyMap::SkyMap(int nside) (skymap.cpp:21-37): RING map of 12 nside^2
+ * pixels on `device`, accumulators zero (the reference leaves them
+ * uninitialised). */
+pisco_status pisco_map_create(int nside, int device, pisco_map** out);
+void pisco_map_destroy(pisco_map* map);
+const char* pisco_map_last_error(const pisco_map* map);
+/* Zero the accumulators. */
+pisco_status pisco_map_reset(pisco_map* map);
+/* SkyMap::accumulate_data(nsamples, ra, dec, pa, ndetectors, detPolAngles,
+ * data) (skymap.cpp:68-132): host arrays of ndet x nsamples values indexed
+ * [det * nsamples + s], dtype FLOAT32 (the reference's type) or FLOAT64;
+ * det_pol_angles: ndet host floats.  psi = -(pol + pa).  Pointings with
+ * |dec| > pi/2 or non-finite values are skipped and reported
+ * (PISCO_ERR_INVALID_ARGUMENT after the rest is accumulated).  Synchronous. */
+pisco_status pisco_map_accumulate(pisco_map* map, long nsamples, const void* ra, const void* dec,
+                                  const void* pa, int ndet, const float* det_pol_angles,
+                                  const void* data, pisco_dtype dtype);
+/* Same from device arrays; runs on `stream` (NULL: the map's own) and
+ * returns when done.  At most 2^31 - 1 values per call. */
+pisco_status pisco_map_accumulate_device(pisco_map* map, long nsamples, const void* d_ra,
+                                         const void* d_dec, const void* d_pa, int ndet,
+                                         const float* det_pol_angles, const void* d_data,
+                                         pisco_dtype dtype, void* stream);
+/* SkyMap::solve_map (skymap.cpp:134-231): per pixel, hits = (int)AtA[0][0];
+ * with hits >= 3 AtA x = AtD is solved (LAPACK dgesv, restated) for
+ * (I, Q, U); an exactly singular system keeps AtD as (I, Q, U) and sets
+ * hits to 0; hits < 3 gives I = Q = U = 0 (INSUFFCOV). */
+pisco_status pisco_map_solve(pisco_map* map);
+/* get_stokes_I / _Q / _U, get_hitmap (skymap.hpp:32-35): host copies of
+ * 12 nside^2 values each (any pointer may be NULL). */
+pisco_status pisco_map_get(pisco_map* map, float* I, float* Q, float* U, int* hits);
+/* The normal equations in the reference's layout: ata = 9 x npix doubles
+ * (AtA row-major per pixel, skymap.cpp:114-122), atd = 3 x npix (either may
+ * be NULL); host copies. */
+pisco_status pisco_map_get_normal(pisco_map* map, double* ata, double* atd);
+/* Device arrays: I, Q, U (3 x npix floats), hits (npix ints) and the normal
+ * equations (9 x npix doubles: AtA[0][0], [0][1], [0][2], [1][1], [1][2],
+ * [2][2], then AtD[0..2], each as one npix-long plane). */
+pisco_status pisco_map_device_arrays(pisco_map* map, const float** d_iqu, const int** d_hits,
+                                     const double** d_normal);
 
 /* ---- host HEALPix / PolBeam helpers (for the C++ PolBeam wrapper) ------ */
 /* Healpix_Base::pix2ang / ang2pix, RING (used by polbeam.cpp:130,441). */

@@ -313,3 +313,81 @@ def ref_rho_sigma_chi(*args):
 
 def refdev_rho_sigma_chi(*args):
     return _rsc(refdev_lib(), "refdev_rho_sigma_chi", *args)
+
+
+# ---------------------------------------------------------------- binned map-making
+def map_accumulate(nside, ra, dec, pa, pol, data, ata=None, atd=None):
+    """SkyMap::accumulate_data restated (skymap.cpp:68-132).  ra, dec, pa,
+    data: (ndet, nsamples) float32 (the reference's types) or float64; pol:
+    ndet floats.  Accumulates into and returns (ata 9 x npix, atd 3 x npix),
+    interleaved per pixel like the reference's AtA / AtD."""
+    npix = 12 * nside * nside
+    f64 = np.asarray(ra).dtype == np.float64
+    dt = np.float64 if f64 else np.float32
+    ra, dec, pa, data = (np.ascontiguousarray(np.atleast_2d(x), dtype=dt) for x in (ra, dec, pa, data))
+    ndet, ns = ra.shape
+    pol = np.ascontiguousarray(pol, dtype=np.float32).reshape(ndet)
+    if ata is None:
+        ata = np.zeros(9 * npix, np.float64)
+    if atd is None:
+        atd = np.zeros(3 * npix, np.float64)
+    fn = lib().orc_map_accumulate_f64 if f64 else lib().orc_map_accumulate_f32
+    fn(_i64(nside), _i64(ns), _ptr(ra), _ptr(dec), _ptr(pa), ctypes.c_int(ndet), _ptr(pol),
+       _ptr(data), _ptr(ata), _ptr(atd))
+    return ata, atd
+
+
+def map_solve(ata, atd):
+    """SkyMap::solve_map restated (skymap.cpp:134-231): (I, Q, U, hits)."""
+    ata = np.ascontiguousarray(ata, np.float64)
+    atd = np.ascontiguousarray(atd, np.float64)
+    npix = atd.size // 3
+    out = [np.empty(npix, np.float32) for _ in range(3)]
+    hits = np.empty(npix, np.int32)
+    lib().orc_map_solve(_i64(npix), _ptr(ata), _ptr(atd), *[_ptr(o) for o in out], _ptr(hits))
+    return out[0], out[1], out[2], hits
+
+
+def dgesv3(a, b):
+    """LAPACK dgesv restated for one 3 x 3 system: (info, x, lu, ipiv); a is
+    the matrix (row-major input, passed column-major as Fortran expects)."""
+    A = np.asfortranarray(np.array(a, np.float64)).ravel(order="F").copy()
+    B = np.array(b, np.float64).copy()
+    ip = np.zeros(3, np.int32)
+    info = lib().orc_dgesv3(_ptr(A), _ptr(ip), _ptr(B))
+    return info, B, A.reshape(3, 3, order="F"), ip
+
+
+REFMAP_LIB = os.path.join(HERE, "_ref", "libpisco_refmap.so")
+REFMAP_EXACT_LIB = os.path.join(HERE, "_ref", "libpisco_refmap_exact.so")
+_refmap = {}
+
+
+def refmap_available() -> bool:
+    return os.path.exists(REFMAP_LIB) and os.path.exists(REFMAP_EXACT_LIB)
+
+
+def ref_skymap(nside, ra, dec, pa, pol, data, ncalls=1, exact=False):
+    """The reference SkyMap (skymap.cpp, compiled unmodified; exact=True: the
+    build without floating-point contraction): ncalls x accumulate_data on
+    the same float32 (ndet, nsamples) arrays, then solve_map.  Returns
+    (ata, atd, I, Q, U, hits)."""
+    path = REFMAP_EXACT_LIB if exact else REFMAP_LIB
+    if path not in _refmap:
+        L = ctypes.CDLL(path)
+        L.ref_skymap_run.restype = ctypes.c_int
+        _refmap[path] = L
+    ra, dec, pa, data = (np.ascontiguousarray(np.atleast_2d(x), dtype=np.float32)
+                         for x in (ra, dec, pa, data))
+    ndet, ns = ra.shape
+    pol = np.ascontiguousarray(pol, dtype=np.float32).reshape(ndet)
+    npix = 12 * nside * nside
+    ata = np.empty(9 * npix, np.float64)
+    atd = np.empty(3 * npix, np.float64)
+    I, Q, U = (np.empty(npix, np.float32) for _ in range(3))
+    hits = np.empty(npix, np.int32)
+    _refmap[path].ref_skymap_run(ctypes.c_int(nside), ctypes.c_int(ns), _ptr(ra), _ptr(dec),
+                                 _ptr(pa), ctypes.c_int(ndet), _ptr(pol), _ptr(data),
+                                 ctypes.c_int(ncalls), _ptr(ata), _ptr(atd), _ptr(I), _ptr(Q),
+                                 _ptr(U), _ptr(hits))
+    return ata, atd, I, Q, U, hits

@@ -7,6 +7,9 @@
 #                        unmodified with the reference's CPU flags
 #                        (CMakeLists.txt:27,37-39) against the HEALPix shim
 #                        in oracle/shim/ (Healpix C++ itself is absent).
+#   libpisco_refmap.so : the binned map-maker SkyMap (skymap.cpp), same flags;
+#   libpisco_refmap_exact.so: the same without floating-point contraction;
+#                        LAPACK's dgesv_ is the oracle's restatement.
 #   libpisco_refdev.so : the reference's device HEALPix port and device
 #                        rotation (cudaHealpix.cu, cudaSphtransf.cu)
 #                        compiled for the host with __device__ removed.
@@ -30,10 +33,22 @@ wait
 g++ -shared -fopenmp -o "$OUT/libpisco_ref.so" "$OUT"/obj/convolver.o "$OUT"/obj/sky.o \
     "$OUT"/obj/scan.o "$OUT"/obj/polbeam.o "$OUT"/obj/sphtrigo.o "$OUT"/obj/ref_harness.o \
     "$OUT"/obj/oracle.o
+# binned map-maker (src/SkyMap/skymap.cpp): with the reference's flags, and
+# once more without floating-point contraction (a bit-exact pin of the
+# oracle's restatement); skymap.cpp uses std::cerr and malloc without their
+# headers, which -include supplies.
+MAPF="-include iostream -include cstdlib -include cstdio -include cmath"
+g++ $CXXF $MAPF -c "$REF/src/SkyMap/skymap.cpp" -o "$OUT/obj/skymap.o"
+g++ $CXXF $MAPF -ffp-contract=off -c "$REF/src/SkyMap/skymap.cpp" -o "$OUT/obj/skymap_exact.o"
+g++ $CXXF -c "$HERE/ref_map_harness.cpp" -o "$OUT/obj/ref_map_harness.o"
+g++ -shared -fopenmp -o "$OUT/libpisco_refmap.so" "$OUT"/obj/skymap.o "$OUT"/obj/ref_map_harness.o \
+    "$OUT"/obj/oracle.o
+g++ -shared -fopenmp -o "$OUT/libpisco_refmap_exact.so" "$OUT"/obj/skymap_exact.o \
+    "$OUT"/obj/ref_map_harness.o "$OUT"/obj/oracle.o
 DEVF="-O2 -fPIC -w -x c++ -D__device__= -include cmath -include math.h -I$REF/src -I$REF/src/GpuConvolver/cuda -I$CUDA_INC"
 g++ $DEVF -c "$REF/src/GpuConvolver/cuda/cudaHealpix.cu" -o "$OUT/obj/cudaHealpix.o"
 g++ $DEVF -c "$REF/src/GpuConvolver/cuda/cudaSphtransf.cu" -o "$OUT/obj/cudaSphtransf.o"
 g++ -O2 -fPIC -w -I$REF/src -I$CUDA_INC -D__device__= -c "$HERE/refdev_harness.cpp" -o "$OUT/obj/refdev_harness.o"
 g++ -shared -o "$OUT/libpisco_refdev.so" "$OUT"/obj/cudaHealpix.o "$OUT"/obj/cudaSphtransf.o \
     "$OUT"/obj/refdev_harness.o
-echo "build_ref.sh: built $OUT/libpisco_ref.so and $OUT/libpisco_refdev.so"
+echo "build_ref.sh: built $OUT/libpisco_ref.so, libpisco_refmap*.so and libpisco_refdev.so"

@@ -751,3 +751,144 @@ void orc_adjoint_f64(int64_t ns, const double* ra, const double* dec,
     }
     free(rg);
 }
+
+/* ---------------- binned map-making (skymap.cpp:68-231) ---------------- */
+
+/* One TOD value into the normal equations of its pixel (skymap.cpp:99-122). */
+static void o_map_add(double* ata, double* atd, int64_t p, double pol, double pa, double d)
+{
+    const double psi = -(pol + pa);
+    const double twopsi = 2.0 * psi;
+    const double c = cos(twopsi), s = sin(twopsi);
+    double* D = atd + 3 * p;
+    double* A = ata + 9 * p;
+    D[0] += 1.0 * d;
+    D[1] += c * d;
+    D[2] += s * d;
+    A[0] += 1.0;
+    A[1] += c;
+    A[2] += s;
+    A[3] += c;
+    A[4] += c * c;
+    A[5] += c * s;
+    A[6] += s;
+    A[7] += c * s;
+    A[8] += s * s;
+}
+
+void orc_map_accumulate_f32(int64_t nside, int64_t ns, const float* ra, const float* dec,
+                            const float* pa, int ndet, const float* pol, const float* data,
+                            double* ata, double* atd)
+{
+    orc_hpx h;
+    orc_hpx_init(&h, nside);
+    for (int d = 0; d < ndet; ++d)
+        for (int64_t i = 0; i < ns; ++i) {
+            const int64_t k = (int64_t)d * ns + i;
+            const int64_t p = orc_ang2pix(&h, O_HALFPI - (double)dec[k], (double)ra[k]);
+            o_map_add(ata, atd, p, (double)pol[d], (double)pa[k], (double)data[k]);
+        }
+}
+
+void orc_map_accumulate_f64(int64_t nside, int64_t ns, const double* ra, const double* dec,
+                            const double* pa, int ndet, const float* pol, const double* data,
+                            double* ata, double* atd)
+{
+    orc_hpx h;
+    orc_hpx_init(&h, nside);
+    for (int d = 0; d < ndet; ++d)
+        for (int64_t i = 0; i < ns; ++i) {
+            const int64_t k = (int64_t)d * ns + i;
+            const int64_t p = orc_ang2pix(&h, O_HALFPI - dec[k], ra[k]);
+            o_map_add(ata, atd, p, (double)pol[d], pa[k], data[k]);
+        }
+}
+
+/* Column-major element (r, c) of a 3 x 3 matrix, 0-based. */
+#define O_A(r, c) a[(c) * 3 + (r)]
+
+int orc_dgesv3(double* a, int* ipiv, double* b)
+{
+    const double sfmin = 2.2250738585072014e-308; /* safe minimum: 1/sfmin does not overflow */
+    int info = 0;
+    /* dgetf2 */
+    for (int j = 0; j < 3; ++j) {
+        int jp = j;
+        double amax = fabs(O_A(j, j));
+        for (int i = j + 1; i < 3; ++i)
+            if (fabs(O_A(i, j)) > amax) {
+                amax = fabs(O_A(i, j));
+                jp = i;
+            }
+        ipiv[j] = jp + 1;
+        if (O_A(jp, j) != 0.0) {
+            if (jp != j)
+                for (int c = 0; c < 3; ++c) {
+                    const double t = O_A(j, c);
+                    O_A(j, c) = O_A(jp, c);
+                    O_A(jp, c) = t;
+                }
+            if (fabs(O_A(j, j)) >= sfmin) {
+                const double r = 1.0 / O_A(j, j);
+                for (int i = j + 1; i < 3; ++i) O_A(i, j) *= r;
+            } else {
+                for (int i = j + 1; i < 3; ++i) O_A(i, j) /= O_A(j, j);
+            }
+        } else if (info == 0) {
+            info = j + 1;
+        }
+        /* rank-1 update of the trailing block: a(i, c) += a(i, j) * (-a(j, c)) */
+        for (int c = j + 1; c < 3; ++c) {
+            if (O_A(j, c) != 0.0) {
+                const double t = -O_A(j, c);
+                for (int i = j + 1; i < 3; ++i) O_A(i, c) += O_A(i, j) * t;
+            }
+        }
+    }
+    if (info != 0) return info;
+    /* dgetrs: interchanges, then L y = P b (unit lower), then U x = y */
+    for (int i = 0; i < 3; ++i) {
+        const int ip = ipiv[i] - 1;
+        if (ip != i) {
+            const double t = b[i];
+            b[i] = b[ip];
+            b[ip] = t;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        if (b[k] != 0.0)
+            for (int i = k + 1; i < 3; ++i) b[i] -= b[k] * O_A(i, k);
+    for (int k = 2; k >= 0; --k)
+        if (b[k] != 0.0) {
+            b[k] /= O_A(k, k);
+            for (int i = 0; i < k; ++i) b[i] -= b[k] * O_A(i, k);
+        }
+    return 0;
+}
+#undef O_A
+
+void orc_map_solve(int64_t npix, const double* ata, const double* atd, float* I, float* Q,
+                   float* U, int* hits)
+{
+    for (int64_t p = 0; p < npix; ++p) {
+        double a[9], b[3];
+        int ipiv[3];
+        /* column-major assembly as skymap.cpp:158-170 (AtA is symmetric) */
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) a[c * 3 + r] = ata[9 * p + 3 * r + c];
+        for (int k = 0; k < 3; ++k) b[k] = atd[3 * p + k];
+        double ii = 0.0, qq = 0.0, uu = 0.0;
+        int h = (int)ata[9 * p];
+        if (h >= 3) {
+            const int info = orc_dgesv3(a, ipiv, b);
+            ii = b[0];
+            qq = b[1];
+            uu = b[2];
+            if (info != 0) h = 0;
+        }
+        I[p] = (float)ii;
+        Q[p] = (float)qq;
+        U[p] = (float)uu;
+        hits[p] = h;
+    }
+}

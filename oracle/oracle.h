@@ -137,6 +137,38 @@ void orc_adjoint_f64(int64_t nsamples, const double* ra, const double* dec,
                      const double* beam_b, const double* g_a,
                      const double* g_b, double* gsky);
 
+/* ---------------- binned map-making (src/SkyMap/skymap.cpp) ---------------- */
+/* SkyMap::accumulate_data (skymap.cpp:68-132).  Arrays indexed
+ * [det * nsamples + s]; for every (det, s) in that order, in double:
+ *   pixel = ang2pix(pi/2 - dec, ra), psi = -(pol[det] + pa), c = cos 2psi,
+ *   s = sin 2psi, AtD[3p..] += (d, c d, s d),
+ *   AtA[9p..] += (1, c, s, c, c c, c s, s, c s, s s).
+ * ata (9 x npix) and atd (3 x npix) are accumulated into (the caller zeroes
+ * them first: the reference's constructor leaves them uninitialised). */
+void orc_map_accumulate_f32(int64_t nside, int64_t nsamples, const float* ra, const float* dec,
+                            const float* pa, int ndet, const float* pol, const float* data,
+                            double* ata, double* atd);
+void orc_map_accumulate_f64(int64_t nside, int64_t nsamples, const double* ra, const double* dec,
+                            const double* pa, int ndet, const float* pol, const double* data,
+                            double* ata, double* atd);
+/* LAPACK dgesv for one 3 x 3 system (the reference links it at
+ * skymap.cpp:13-19 and calls it at :186-193; LAPACK is not in the reference
+ * tree and its version is unpinned).  Restates the published reference
+ * LAPACK/BLAS algorithm: dgetf2 (unblocked LU, partial pivoting by the first
+ * largest |a|, multipliers by the reciprocal of the pivot when it is at least
+ * the safe minimum, rank-1 updates a + l (-u)), then, only when no pivot is
+ * exactly zero, dgetrs (row interchanges; unit-lower and upper triangular
+ * solves, column-oriented as the reference dtrsm).  a: column-major 3 x 3,
+ * overwritten with the factors; b: right-hand side, overwritten with the
+ * solution (unchanged when info != 0).  Returns info (0, or k if U(k,k) is
+ * exactly zero, 1-based). */
+int orc_dgesv3(double* a, int* ipiv, double* b);
+/* SkyMap::solve_map (skymap.cpp:134-231): per pixel, hits = (int)AtA[0];
+ * hits >= 3: solve AtA x = AtD (dgesv); x to I, Q, U; a singular system
+ * keeps AtD as I, Q, U and sets hits to 0.  hits < 3: I = Q = U = 0. */
+void orc_map_solve(int64_t npix, const double* ata, const double* atd, float* I, float* Q,
+                   float* U, int* hits);
+
 #ifdef __cplusplus
 }
 #endif

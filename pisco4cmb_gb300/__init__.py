@@ -2,12 +2,13 @@
 
 A drop-in for the convolution path of PISCO (pafluxa/pisco4cmb): Scan
 pointing, Sky I/Q/U/V HEALPix maps and PolBeam Stokes beam maps in, detector
-a/b time-ordered data out.  The compute path is libpisco_gb300.so
+a/b time-ordered data out; and the binned map-maker that turns TOD back into
+I, Q, U maps (SkyMap).  The compute path is libpisco_gb300.so
 (hand-written sm_103a CUDA behind a C ABI, include/pisco_gb300.h); this
 package is its host-side mirror of the reference API.
 """
 from .api import (Convolver, GPUConvolver, PiscoError, PiscoInvalidArgument, PolBeam,  # noqa: F401
-                  RunConfig, Scan, Sky, ang2pix, beam_npix_for_radius, pix2ang)
+                  RunConfig, Scan, Sky, SkyMap, ang2pix, beam_npix_for_radius, pix2ang)
 
 __all__ = ["Convolver", "GPUConvolver", "PiscoError", "PiscoInvalidArgument", "PolBeam",
-           "RunConfig", "Scan", "Sky", "ang2pix", "beam_npix_for_radius", "pix2ang"]
+           "RunConfig", "Scan", "Sky", "SkyMap", "ang2pix", "beam_npix_for_radius", "pix2ang"]

@@ -126,6 +126,17 @@ SIGNATURES = [
     ("pisco_beam_gaussian_fields", _S, [_I, _L, _D, _D, _D, _P, _P, _P, _P]),
     ("pisco_beam_from_fields", _S, [_L, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("pisco_beam_build", _S, [_I, _L, _D, ctypes.c_char, _I, _PP, _PP, _PP, _PP]),
+    ("pisco_map_create", _S, [_I, _I, ctypes.POINTER(_P)]),
+    ("pisco_map_destroy", None, [_P]),
+    ("pisco_map_last_error", ctypes.c_char_p, [_P]),
+    ("pisco_map_reset", _S, [_P]),
+    ("pisco_map_accumulate", _S, [_P, _L, _P, _P, _P, _I, _P, _P, _I]),
+    ("pisco_map_accumulate_device", _S, [_P, _L, _P, _P, _P, _I, _P, _P, _I, _P]),
+    ("pisco_map_solve", _S, [_P]),
+    ("pisco_map_get", _S, [_P, _P, _P, _P, _P]),
+    ("pisco_map_get_normal", _S, [_P, _P, _P]),
+    ("pisco_map_device_arrays", _S, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                     ctypes.POINTER(_P)]),
 ]
 
 _lib = None

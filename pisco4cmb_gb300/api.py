@@ -28,8 +28,8 @@ from . import _lib
 from ._lib import (FLOAT32, FLOAT64, FORMS, PiscoError, PiscoInvalidArgument, RunConfig,
                    check, load, ptr_array)
 
-__all__ = ["Scan", "Sky", "PolBeam", "Convolver", "GPUConvolver", "RunConfig", "PiscoError",
-           "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix"]
+__all__ = ["Scan", "Sky", "PolBeam", "Convolver", "GPUConvolver", "SkyMap", "RunConfig",
+           "PiscoError", "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix"]
 
 
 def _ptr(a: np.ndarray):
@@ -320,12 +320,15 @@ class GPUConvolver:
 
     def adjoint_device(self, d_ga: int, d_gb: int, g_f64: bool, d_gsky: int, d_gbeam: int,
                        out_f64: bool = False, deterministic: bool = True, begin: int = 0,
-                       n: int | None = None, stream: int = 0) -> None:
+                       n: int | None = None, stream: int = 0, sky_iqu: bool = False) -> None:
+        """sky_iqu: accumulate I, Q, U only (the V column of the sky gradient
+        is written as zero)."""
         n = self._n - begin if n is None else n
+        mode = (1 if deterministic else 0) | (2 if sky_iqu else 0)
         check(load().pisco_adjoint_device(self.ctx, begin, n, d_ga, d_gb,
                                           FLOAT64 if g_f64 else FLOAT32, d_gsky or None,
                                           d_gbeam or None, FLOAT64 if out_f64 else FLOAT32,
-                                          1 if deterministic else 0, stream or None),
+                                          mode, stream or None),
               self.ctx, "adjoint_device")
 
     def adjoint(self, g_a: np.ndarray, g_b: np.ndarray, deterministic: bool = True,
@@ -417,3 +420,126 @@ class Convolver:
                                data_b if polFlag in "bp" else None, polFlag=polFlag)
         finally:
             g.close()
+
+
+class SkyMap:
+    """Binned map-maker, SkyMap (src/SkyMap/skymap.hpp:13-56), on the GPU.
+
+    ``accumulate_data`` adds TOD into per-pixel normal equations (FP64,
+    device-resident, each pixel's totals in the reference's order);
+    ``solve_map`` solves them for I, Q, U (``get_stokes_I`` ...,
+    ``get_hitmap``).  The accumulators start at zero."""
+
+    INSUFFCOV = 0
+
+    def __init__(self, nside: int, device: int = 0):
+        L = load()
+        h = ctypes.c_void_p()
+        st = L.pisco_map_create(int(nside), int(device), ctypes.byref(h))
+        if st != _lib.PISCO_OK:
+            text = "SkyMap(%d): %s" % (nside, L.pisco_status_string(st).decode())
+            if st == _lib.PISCO_ERR_INVALID_ARGUMENT:
+                raise PiscoInvalidArgument(st, text)
+            raise PiscoError(st, text)
+        self._h = h
+        self.nside = int(nside)
+        self.nPixels = 12 * self.nside * self.nside
+        self._out = None
+
+    def _check(self, st: int, what: str) -> None:
+        if st == _lib.PISCO_OK:
+            return
+        L = load()
+        text = "%s: %s (%s)" % (what, L.pisco_map_last_error(self._h).decode(),
+                                L.pisco_status_string(st).decode())
+        if st == _lib.PISCO_ERR_INVALID_ARGUMENT:
+            raise PiscoInvalidArgument(st, text)
+        raise PiscoError(st, text)
+
+    def get_nside(self) -> int:
+        return self.nside
+
+    def size(self) -> int:
+        return self.nPixels
+
+    def reset(self) -> None:
+        self._check(load().pisco_map_reset(self._h), "reset")
+        self._out = None
+
+    def accumulate_data(self, nsamples: int, ra, dec, pa, ndetectors: int, detPolAngles, data):
+        """Host arrays of ndetectors x nsamples values ([det * nsamples + s],
+        or shape (ndetectors, nsamples)), float32 as in the reference or
+        float64; detPolAngles: ndetectors angles (radians)."""
+        f64 = np.asarray(ra).dtype == np.float64
+        dt = np.float64 if f64 else np.float32
+        arrs = [np.ascontiguousarray(np.asarray(x).reshape(-1), dtype=dt) for x in (ra, dec, pa, data)]
+        n = int(nsamples) * int(ndetectors)
+        if any(a.size != n for a in arrs):
+            raise PiscoInvalidArgument(1, "accumulate_data: arrays must hold ndetectors x nsamples values")
+        pol = np.ascontiguousarray(detPolAngles, dtype=np.float32).reshape(-1)
+        if pol.size != int(ndetectors):
+            raise PiscoInvalidArgument(1, "accumulate_data: one polarisation angle per detector")
+        self._check(load().pisco_map_accumulate(self._h, int(nsamples), *[_ptr(a) for a in arrs[:3]],
+                                                int(ndetectors), _ptr(pol), _ptr(arrs[3]),
+                                                FLOAT64 if f64 else FLOAT32), "accumulate_data")
+        self._out = None
+
+    def accumulate_device(self, nsamples: int, d_ra: int, d_dec: int, d_pa: int, ndetectors: int,
+                          detPolAngles, d_data: int, f64: bool = False, stream: int = 0) -> None:
+        """Device arrays (pointers) of ndetectors x nsamples values."""
+        pol = np.ascontiguousarray(detPolAngles, dtype=np.float32).reshape(-1)
+        self._check(load().pisco_map_accumulate_device(self._h, int(nsamples), d_ra, d_dec, d_pa,
+                                                       int(ndetectors), _ptr(pol), d_data,
+                                                       FLOAT64 if f64 else FLOAT32, stream or None),
+                    "accumulate_device")
+        self._out = None
+
+    def solve_map(self) -> None:
+        self._check(load().pisco_map_solve(self._h), "solve_map")
+        self._out = None
+
+    def _fetch(self):
+        if self._out is None:
+            I, Q, U = (np.empty(self.nPixels, np.float32) for _ in range(3))
+            hits = np.empty(self.nPixels, np.int32)
+            self._check(load().pisco_map_get(self._h, _ptr(I), _ptr(Q), _ptr(U), _ptr(hits)),
+                        "get maps")
+            self._out = (I, Q, U, hits)
+        return self._out
+
+    def get_stokes_I(self) -> np.ndarray:
+        return self._fetch()[0]
+
+    def get_stokes_Q(self) -> np.ndarray:
+        return self._fetch()[1]
+
+    def get_stokes_U(self) -> np.ndarray:
+        return self._fetch()[2]
+
+    def get_hitmap(self) -> np.ndarray:
+        return self._fetch()[3]
+
+    def get_normal(self):
+        """(AtA 9 x npix, AtD 3 x npix) host copies in the reference's layout."""
+        ata = np.empty(9 * self.nPixels, np.float64)
+        atd = np.empty(3 * self.nPixels, np.float64)
+        self._check(load().pisco_map_get_normal(self._h, _ptr(ata), _ptr(atd)), "get_normal")
+        return ata, atd
+
+    def device_arrays(self):
+        """(d_iqu, d_hits, d_normal) device pointers (see pisco_map_device_arrays)."""
+        a, b, c = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(load().pisco_map_device_arrays(self._h, ctypes.byref(a), ctypes.byref(b),
+                                                   ctypes.byref(c)), "device_arrays")
+        return a.value, b.value, c.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            try:
+                load().pisco_map_destroy(self._h)
+            except Exception:  # noqa: BLE001 -- interpreter shutdown
+                pass
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -66,10 +66,12 @@ class ConvolveFn(torch.autograd.Function):
         gsky = torch.empty((sky4.shape[0], 4), dtype=torch.float64, device=sky4.device) if want_sky else None
         gbeam = torch.empty((bab.shape[0], 8), dtype=torch.float64, device=sky4.device) if want_beam else None
         if want_sky or want_beam:
+            # an I, Q, U sky has no V gradient to accumulate
+            iqu = len(sky_shape) == 2 and 3 in tuple(sky_shape)
             conv.adjoint_device(ga.data_ptr(), gb.data_ptr(), g64,
                                 gsky.data_ptr() if gsky is not None else 0,
                                 gbeam.data_ptr() if gbeam is not None else 0, out_f64=True,
-                                deterministic=det, stream=stream)
+                                deterministic=det, stream=stream, sky_iqu=iqu)
         if gsky is not None:
             gsky = _like_sky(gsky, sky_shape).to(sky_dtype)
         if gbeam is not None:

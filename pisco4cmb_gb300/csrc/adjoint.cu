@@ -40,6 +40,7 @@ struct Scatter {
     unsigned long long* gbeam_fx;
     const float4* sky;            // for the beam gradient
     double ssky, sbeam;           // fixed-point scales 2^S
+    int want_v;                   // accumulate the V column
 
     __device__ __forceinline__ static unsigned long long fx(double v, double scale)
     {
@@ -56,7 +57,8 @@ struct Scatter {
     {
         scatter(p.ga, p.gb, pix, B, c2, s2);
     }
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2) const
+    __device__ __forceinline__ int fetch(int) const { return 0; }
+    __device__ __forceinline__ void pair(int pix, int, const F8& B, float c2, float s2) const
     {
         scatter(ga, gb, pix, B, c2, s2);
     }
@@ -67,13 +69,13 @@ struct Scatter {
         const float gI = wa * B.a.x + wb * B.b.x;
         const float gQ = wa * (B.a.y * c2 - B.a.z * s2) + wb * (-B.b.y * c2 + B.b.z * s2);
         const float gU = wa * (B.a.z * c2 + B.a.y * s2) + wb * (-B.b.z * c2 - B.b.y * s2);
-        const float gV = wa * B.a.w + wb * B.b.w;
+        const float gV = want_v ? wa * B.a.w + wb * B.b.w : 0.0f;
         if (kFixed) {
             unsigned long long* p = gsky_fx + 4ll * pix;
             atomicAdd(p + 0, fx(gI, ssky));
             atomicAdd(p + 1, fx(gQ, ssky));
             atomicAdd(p + 2, fx(gU, ssky));
-            atomicAdd(p + 3, fx(gV, ssky));
+            if (want_v) atomicAdd(p + 3, fx(gV, ssky));
         } else {
             atomicAdd(reinterpret_cast<float4*>(gsky) + pix, make_float4(gI, gQ, gU, gV));
         }
@@ -94,6 +96,7 @@ struct ScatterBeam {
     unsigned long long* gbeam_fx;
     double ssky, sbeam;
     int want_sky;
+    int want_v;
 
     __device__ __forceinline__ void stash(tuned::Pend& p) const
     {
@@ -103,22 +106,24 @@ struct ScatterBeam {
     __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, float c2,
                                             float s2, float&, float&) const
     {
-        scatter(p.ga, p.gb, pix, B, c2, s2);
+        scatter(p.ga, p.gb, pix, fetch(pix), B, c2, s2);
     }
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2) const
+    __device__ __forceinline__ float4 fetch(int pix) const { return __ldg(&sky[pix]); }
+    __device__ __forceinline__ void pair(int pix, const float4& S, const F8& B, float c2,
+                                         float s2) const
     {
-        scatter(ga, gb, pix, B, c2, s2);
+        scatter(ga, gb, pix, S, B, c2, s2);
     }
 
-    __device__ __forceinline__ void scatter(float wa, float wb, int pix, const F8& B, float c2,
-                                           float s2) const
+    __device__ __forceinline__ void scatter(float wa, float wb, int pix, const float4& S,
+                                           const F8& B, float c2, float s2) const
     {
         if (want_sky) {
-            const Scatter<kFixed> sc{wa, wb, gsky, gsky_fx, nullptr, nullptr, nullptr, ssky, sbeam};
-            sc.pair(pix, B, c2, s2);
+            const Scatter<kFixed> sc{wa,      wb,   gsky,  gsky_fx, nullptr,
+                                     nullptr, nullptr, ssky, sbeam, want_v};
+            sc.scatter(wa, wb, pix, B, c2, s2);
         }
         const long long bp = &B - beam_base;
-        const float4 S = __ldg(&sky[pix]);
         const float qa = S.y * c2 + S.z * s2, ua = S.z * c2 - S.y * s2;
         const float v[8] = {wa * S.x, wa * qa, wa * ua, wa * S.w, wb * S.x, -wb * qa, -wb * ua, wb * S.w};
         if (kFixed) {
@@ -271,19 +276,22 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st)
     const bool beam = a.gbeam32 || a.gbeam_fx;
     if (a.fixed) {
         if (beam) {
-            ScatterBeam<true> act{0, 0, a.beam32, a.sky32, nullptr, a.gsky_fx, nullptr, a.gbeam_fx,
-                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr};
+            ScatterBeam<true> act{0,          0,         a.beam32,     a.sky32,
+                                  nullptr,    a.gsky_fx, nullptr,      a.gbeam_fx,
+                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr, a.want_v};
             return launch_act(a, act, sm_count, st);
         }
-        Scatter<true> act{0, 0, nullptr, a.gsky_fx, nullptr, nullptr, a.sky32, a.sky_scale, a.beam_scale};
+        Scatter<true> act{0,       0,       nullptr,     a.gsky_fx,    nullptr,
+                          nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v};
         return launch_act(a, act, sm_count, st);
     }
     if (beam) {
-        ScatterBeam<false> act{0, 0, a.beam32, a.sky32, a.gsky32, nullptr, a.gbeam32, nullptr,
-                               0.0, 0.0, a.gsky32 != nullptr};
+        ScatterBeam<false> act{0,         0,       a.beam32, a.sky32, a.gsky32,
+                               nullptr,   a.gbeam32, nullptr, 0.0,   0.0,
+                               a.gsky32 != nullptr, a.want_v};
         return launch_act(a, act, sm_count, st);
     }
-    Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0};
+    Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0, a.want_v};
     return launch_act(a, act, sm_count, st);
 }
 

@@ -118,8 +118,10 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     if ((g_dtype != PISCO_FLOAT32 && g_dtype != PISCO_FLOAT64) ||
         (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64))
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
-    if (mode != PISCO_ADJ_ATOMIC && mode != PISCO_ADJ_DETERMINISTIC)
+    if ((int)mode & ~(PISCO_ADJ_DETERMINISTIC | PISCO_ADJ_SKY_IQU))
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad adjoint mode");
+    const bool deterministic = ((int)mode & PISCO_ADJ_DETERMINISTIC) != 0;
+    const bool sky_iqu = ((int)mode & PISCO_ADJ_SKY_IQU) != 0;
     if (!tuned_supported(c->nside_beam, (int)c->npix_beam, c->rho_max))
         return fail(c, PISCO_ERR_UNSUPPORTED, "beam outside the adjoint's (TUNED) domain");
     pisco_status st = c->activate();
@@ -144,12 +146,13 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     a.g_a = d_ga;
     a.g_b = d_gb;
     a.g_f64 = g_dtype == PISCO_FLOAT64;
+    a.want_v = sky_iqu ? 0 : 1;
     st = c->range_order(begin, n, s, &a.order);
     if (st != PISCO_OK) return st;
     a.err = c->d_err;
     a.fallbacks = c->d_fallbacks;
     CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
-    if (mode == PISCO_ADJ_ATOMIC) {
+    if (!deterministic) {
         a.fixed = 0;
         float* gs = nullptr;
         float* gbm = nullptr;

@@ -138,6 +138,7 @@ struct AdjArgs {
     float* gbeam32;                // atomic: [npixB][8] or null
     unsigned long long* gbeam_fx;  // fixed: [npixB][8] or null
     double sky_scale, beam_scale;  // fixed-point scales 2^S
+    int want_v;                    // accumulate the sky gradient's V column
     unsigned int* err;
     unsigned long long* fallbacks;
 };

@@ -41,7 +41,8 @@
 // adjoint.cu):
 //   kSums                     true: per-sample sums, TOD written per sample
 //   void reset(), total(a, b) main-pass sums (kSums)
-//   void pair(int pix, const F8& beam, float c2, float s2)
+//   P fetch(int pix)          per-pixel data (loaded before the pair's geometry)
+//   void pair(int pix, P fetched, const F8& beam, float c2, float s2)
 //   void stash(Pend&)         per-sample data a queued pair needs later
 //   void deferred(const Pend&, int pix, const F8& beam, float c2, float s2,
 //                 float& ta, float& tb)      a re-evaluated pair
@@ -338,16 +339,16 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
     const bool swap = y > x;
     const float mn = swap ? x : y, mx = swap ? y : x;
     const float t = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
-    const float t2 = t * t;
-    float p = 0.0028662257f;
-    p = fmaf(p, t2, -0.0161657367f);
-    p = fmaf(p, t2, 0.0429096138f);
-    p = fmaf(p, t2, -0.0752896400f);
-    p = fmaf(p, t2, 0.1065626393f);
-    p = fmaf(p, t2, -0.1420889944f);
-    p = fmaf(p, t2, 0.1999355085f);
-    p = fmaf(p, t2, -0.3333314528f);
-    p = fmaf(p, t2, 1.0f);
+    // p(s) = sum_k c_k s^k, s = t^2, by Estrin's scheme (5 dependent steps
+    // instead of Horner's 9)
+    const float t2 = t * t, t4 = t2 * t2, t8 = t4 * t4, t16 = t8 * t8;
+    const float q0 = fmaf(-0.3333314528f, t2, 1.0f);
+    const float q1 = fmaf(-0.1420889944f, t2, 0.1999355085f);
+    const float q2 = fmaf(-0.0752896400f, t2, 0.1065626393f);
+    const float q3 = fmaf(-0.0161657367f, t2, 0.0429096138f);
+    const float r0 = fmaf(q1, t4, q0);
+    const float r1 = fmaf(q3, t4, q2);
+    const float p = fmaf(0.0028662257f, t16, fmaf(r1, t8, r0));
     const float a = t * p * 0.63661977236758134f;  // atan(t) / (pi/2)
     return swap ? 1.0f - a : a;
 }
@@ -512,6 +513,9 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                 if (pix < 0 || pix >= hs.npix) {
                     record(err, kCheckSkyIndex);
                 } else {
+                    // the action's per-pixel data (the sky) is requested now, so
+                    // its latency overlaps the geometry below
+                    const auto pre = act.fetch(pix);
                     const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
                     const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
                     const float dl = fmaf((float)kk, R0.y, R0.x);
@@ -565,7 +569,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                             const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
                             const float er = fmaf(wr, wr, -wi * wi) * iw;
                             const float ei = 2.0f * wr * wi * iw;
-                            act.pair(pix, B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
+                            act.pair(pix, pre, B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
                                      fmaf(ei, F.c2p, er * F.s2p));
                         }
                     }
@@ -612,19 +616,19 @@ struct Gather {
     const float4* sky;
     float sa, ca, sb, cb;
     __device__ __forceinline__ void reset() { sa = ca = sb = cb = 0.0f; }
-    __device__ __forceinline__ void contrib(int pix, const F8& B, float c2, float s2, float& ta,
-                                           float& tb) const
+    __device__ __forceinline__ float4 fetch(int pix) const { return __ldg(&sky[pix]); }
+    __device__ __forceinline__ static void contrib(const float4& S, const F8& B, float c2, float s2,
+                                                  float& ta, float& tb)
     {
-        const float4 S = __ldg(&sky[pix]);
         ta = S.x * B.a.x + S.y * (B.a.y * c2 - B.a.z * s2) + S.z * (B.a.z * c2 + B.a.y * s2) +
              S.w * B.a.w;
         tb = S.x * B.b.x + S.y * (-B.b.y * c2 + B.b.z * s2) + S.z * (-B.b.z * c2 - B.b.y * s2) +
              S.w * B.b.w;
     }
-    __device__ __forceinline__ void pair(int pix, const F8& B, float c2, float s2)
+    __device__ __forceinline__ void pair(int, const float4& S, const F8& B, float c2, float s2)
     {
         float ta, tb;
-        contrib(pix, B, c2, s2, ta, tb);
+        contrib(S, B, c2, s2, ta, tb);
         two_sum(sa, ca, ta);
         two_sum(sb, cb, tb);
     }
@@ -632,7 +636,7 @@ struct Gather {
     __device__ __forceinline__ void deferred(const Pend&, int pix, const F8& B, float c2, float s2,
                                             float& ta, float& tb) const
     {
-        contrib(pix, B, c2, s2, ta, tb);
+        contrib(fetch(pix), B, c2, s2, ta, tb);
     }
     // warp total (fixed shuffle tree: deterministic)
     __device__ __forceinline__ void total(double& a, double& b) const

@@ -1,10 +1,12 @@
 // dropin_c1.cpp -- a caller written against the reference API, compiled
 // unchanged against include/pisco (header-only wrappers over the C ABI of
 // libpisco_gb300.so).  Builds the c1 PolBeam, reads the sky and scan from raw
-// float32 files, runs GPUConvolver and Convolver and writes both TODs.
+// float32 files, runs GPUConvolver and Convolver and writes both TODs; with
+// an eighth argument it also maps the GPU TOD of detectors a (0 deg) and b
+// (90 deg) back with SkyMap and writes I, Q, U and the hits (float32 planes).
 //
 // usage: dropin_c1 <nside_sky> <nsamples> sky.f32 (3 planes) scan.f32
-//        (ra, dec, pa planes) out_gpuconv.f32 out_conv.f32
+//        (ra, dec, pa planes) out_gpuconv.f32 out_conv.f32 [out_map.f32]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -16,6 +18,7 @@
 #include "Polbeam/polbeam.hpp"
 #include "Scan/scan.hpp"
 #include "Sky/sky.hpp"
+#include "SkyMap/skymap.hpp"
 
 static std::vector<float> read_f32(const char* path, size_t n)
 {
@@ -38,7 +41,7 @@ static void write_f32(const char* path, const std::vector<float>& v)
 
 int main(int argc, char** argv)
 {
-    if (argc != 7) return 2;
+    if (argc != 7 && argc != 8) return 2;
     const int nsideSky = std::atoi(argv[1]);
     const long ns = std::atol(argv[2]);
     const long npix = 12L * nsideSky * nsideSky;
@@ -91,6 +94,30 @@ int main(int argc, char** argv)
     }
     write_f32(argv[5], out1);
     write_f32(argv[6], out2);
+
+    if (argc == 8) {
+        // two detectors of one pair: same pointing, angles 0 and 90 deg
+        std::vector<float> ra2(2 * ns), dec2(2 * ns), pa2(2 * ns), d2(2 * ns);
+        for (long i = 0; i < ns; ++i)
+            for (int det = 0; det < 2; ++det) {
+                ra2[det * ns + i] = scan[i];
+                dec2[det * ns + i] = scan[ns + i];
+                pa2[det * ns + i] = scan[2 * ns + i];
+                d2[det * ns + i] = det == 0 ? ga[i] : gb[i];
+            }
+        float pol[2] = {0.0f, (float)(M_PI / 2.0)};
+        SkyMap smap(nsideSky);
+        smap.accumulate_data((int)ns, ra2.data(), dec2.data(), pa2.data(), 2, pol, d2.data());
+        smap.solve_map();
+        std::vector<float> m(4 * npix);
+        for (long p = 0; p < npix; ++p) {
+            m[p] = smap.get_stokes_I()[p];
+            m[npix + p] = smap.get_stokes_Q()[p];
+            m[2 * npix + p] = smap.get_stokes_U()[p];
+            m[3 * npix + p] = (float)smap.get_hitmap()[p];
+        }
+        write_f32(argv[7], m);
+    }
     std::printf("dropin ok\n");
     return 0;
 }

@@ -54,15 +54,16 @@ def _fwd(conv, n, form="tuned"):
     return a.cpu().numpy(), b.cpu().numpy()
 
 
-def _adj(conv, ga, gb, deterministic=True, beam=False):
+def _adj(conv, ga, gb, deterministic=True, beam=False, sky_iqu=False):
     import torch
 
     npix = conv._npix_sky
     g = [torch.tensor(x, device="cuda") for x in (ga, gb)]
-    gs = torch.empty((npix, 4), dtype=torch.float64, device="cuda")
+    gs = torch.full((npix, 4), float("nan"), dtype=torch.float64, device="cuda")
     gbm = torch.empty((conv._keep_npb, 8), dtype=torch.float64, device="cuda") if beam else None
     conv.adjoint_device(g[0].data_ptr(), g[1].data_ptr(), True, gs.data_ptr(),
-                        gbm.data_ptr() if beam else 0, out_f64=True, deterministic=deterministic)
+                        gbm.data_ptr() if beam else 0, out_f64=True, deterministic=deterministic,
+                        sky_iqu=sky_iqu)
     conv.sync()
     return gs.cpu().numpy(), (gbm.cpu().numpy() if beam else None)
 
@@ -96,6 +97,26 @@ def test_deterministic_and_atomic_modes(gpu):
     g3, b3 = _adj(conv, ya, yb, False, beam=True)
     assert np.abs(g3 - g1).max() <= 1e-5 * np.abs(g1).max()
     assert np.abs(b3 - b1).max() <= 1e-5 * np.abs(b1).max()
+
+
+def test_sky_iqu_only(gpu):
+    """PISCO_ADJ_SKY_IQU: I, Q, U columns as with V, V column zero."""
+    import torch
+
+    conv, sky, beam, ra, *_ = _case(seed=6)
+    conv._keep_npb = beam.nPixels
+    rng = np.random.default_rng(4)
+    # a beam with V components, so that the full V gradient is not zero
+    d = torch.tensor(rng.normal(size=(beam.nPixels, 8)).astype(np.float32), device="cuda")
+    conv.set_beam_device(beam.nside, beam.nPixels, d.data_ptr())
+    ya, yb = rng.normal(size=ra.size), rng.normal(size=ra.size)
+    full, bfull = _adj(conv, ya, yb, True, beam=True)
+    iqu, biqu = _adj(conv, ya, yb, True, beam=True, sky_iqu=True)
+    assert np.array_equal(full[:, :3], iqu[:, :3]) and np.array_equal(bfull, biqu)
+    assert not np.any(iqu[:, 3]) and np.any(full[:, 3])
+    at, _ = _adj(conv, ya, yb, False, sky_iqu=True)
+    assert not np.any(at[:, 3])
+    assert np.abs(at[:, :3] - full[:, :3]).max() <= 1e-5 * np.abs(full).max()
 
 
 def test_beam_adjoint_is_transpose(gpu):
