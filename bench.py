@@ -685,6 +685,44 @@ def run_order_study(args):
     line = {"workload": "order_c2_nside1024_beam3deg", "nsamples": n, "timings": res,
             "shuffled_sky_over_scan": res["shuffled_scan_order"]["ms"] / res["shuffled_sky_order"]["ms"]}
     print(json.dumps(line), flush=True)
+
+    # a sky larger than L2 (nside 2048: 805 MB) read by uniformly random pointings
+    from pisco4cmb_gb300 import synth
+
+    w = synth.WORKLOADS[3]
+    sky3 = synth.grf_sky(w["nside_sky"], 3, lmax=w["lmax"], dtype=np.float32, device="cuda")
+    beam3 = _gaussian_beam(w["nside_beam"], w["radius_deg"], w["fwhm_deg"], w["ellipticity"],
+                           w["nside_sky"])
+    n3 = 1_000_000
+    rng = np.random.default_rng(20261204)
+    ra3 = rng.uniform(0, 2 * np.pi, n3)
+    dec3 = np.arcsin(rng.uniform(-1, 1, n3))
+    pa3 = rng.uniform(0, np.pi, n3)
+    res3 = {}
+    for order in ("scan", "sky"):
+        c = GPUConvolver(form="tuned")
+        c.update_sky(Sky(w["nside_sky"], sky3[0], sky3[1], sky3[2], None))
+        c.update_beam(beam3)
+        c.update_scan(Scan(n3, ra3, dec3, pa3))
+        c.set_sample_order(order)
+        a = torch.empty(n3, device="cuda")
+        b = torch.empty(n3, device="cuda")
+        for _ in range(2):
+            c.forward_device(a.data_ptr(), b.data_ptr(), stream=cs)
+        c.sync()
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(i & 0xff)
+            e0.record()
+            c.forward_device(a.data_ptr(), b.data_ptr(), stream=cs)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        res3[order] = {"ms": float(np.median(ts)), "samples_per_s": n3 / (np.median(ts) / 1e3)}
+        c.close()
+    line = {"workload": "order_random_fullsky_nside2048_beam1deg", "nsamples": n3, "timings": res3,
+            "sky_over_scan": res3["scan"]["ms"] / res3["sky"]["ms"]}
+    print(json.dumps(line), flush=True)
     return 0
 
 

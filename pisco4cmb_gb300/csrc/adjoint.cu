@@ -26,7 +26,7 @@
 namespace pisco {
 namespace {
 
-constexpr int kAW = 8;
+constexpr int kAW = PISCO_TUNED_WARPS;
 
 // Queued pairs are redone after the sample has moved on, so the weights
 // (ga, gb) of their sample travel in its slot (stash / deferred).

@@ -7,7 +7,7 @@
 // leaves the GPU idle in every tail.  Here the host cuts every detector's
 // samples into chunks, orders the chunks longest-first (estimated pairs),
 // and one kernel whose blocks pull chunks with one atomic each runs them all
-// (the 8 warps of a block share a chunk, sample by sample).
+// (the warps of a block share a chunk, sample by sample).
 // The launch (queue reset + kernel) is captured once in a CUDA graph and
 // replayed while the same detector set is resubmitted.  The chunk size is
 // chosen by the autotuner (pisco_autotune_batched) and cached per workload
@@ -35,7 +35,7 @@ using namespace pisco;
 namespace pisco {
 namespace {
 
-constexpr int kBW = 8;  // warps per block
+constexpr int kBW = PISCO_TUNED_WARPS;  // warps per block
 
 // A block pulls one item at a time and its warps take the item's samples
 // round-robin, so the warps of an SM work on neighbouring samples (whose

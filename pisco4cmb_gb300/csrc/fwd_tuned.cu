@@ -14,7 +14,7 @@
 namespace pisco {
 namespace {
 
-constexpr int kTW = 8;
+constexpr int kTW = PISCO_TUNED_WARPS;
 
 template <bool kCalib>
 __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)

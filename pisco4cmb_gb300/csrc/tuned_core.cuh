@@ -41,7 +41,7 @@
 // adjoint.cu):
 //   kSums                     true: per-sample sums, TOD written per sample
 //   void reset(), total(a, b) main-pass sums (kSums)
-//   P fetch(int pix)          per-pixel data (loaded before the pair's geometry)
+//   P fetch(int pix)          per-pixel data the action needs (Gather: the sky)
 //   void pair(int pix, P fetched, const F8& beam, float c2, float s2)
 //   void stash(Pend&)         per-sample data a queued pair needs later
 //   void deferred(const Pend&, int pix, const F8& beam, float c2, float s2,
@@ -54,8 +54,12 @@
 #include "hpx.cuh"
 #include "internal.h"
 
-// Minimum resident 256-thread blocks per SM requested from the compiler for
-// the kernels built on this core (caps their registers).
+// Warps per block of the kernels built on this core, and the minimum number
+// of resident blocks per SM requested from the compiler (which caps their
+// registers at 65536 / (32 x warps x blocks)).
+#ifndef PISCO_TUNED_WARPS
+#define PISCO_TUNED_WARPS 8
+#endif
 #ifndef PISCO_TUNED_MINB
 #define PISCO_TUNED_MINB 2
 #endif
@@ -339,16 +343,16 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
     const bool swap = y > x;
     const float mn = swap ? x : y, mx = swap ? y : x;
     const float t = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
-    // p(s) = sum_k c_k s^k, s = t^2, by Estrin's scheme (5 dependent steps
-    // instead of Horner's 9)
-    const float t2 = t * t, t4 = t2 * t2, t8 = t4 * t4, t16 = t8 * t8;
-    const float q0 = fmaf(-0.3333314528f, t2, 1.0f);
-    const float q1 = fmaf(-0.1420889944f, t2, 0.1999355085f);
-    const float q2 = fmaf(-0.0752896400f, t2, 0.1065626393f);
-    const float q3 = fmaf(-0.0161657367f, t2, 0.0429096138f);
-    const float r0 = fmaf(q1, t4, q0);
-    const float r1 = fmaf(q3, t4, q2);
-    const float p = fmaf(0.0028662257f, t16, fmaf(r1, t8, r0));
+    const float t2 = t * t;
+    float p = 0.0028662257f;
+    p = fmaf(p, t2, -0.0161657367f);
+    p = fmaf(p, t2, 0.0429096138f);
+    p = fmaf(p, t2, -0.0752896400f);
+    p = fmaf(p, t2, 0.1065626393f);
+    p = fmaf(p, t2, -0.1420889944f);
+    p = fmaf(p, t2, 0.1999355085f);
+    p = fmaf(p, t2, -0.3333314528f);
+    p = fmaf(p, t2, 1.0f);
     const float a = t * p * 0.63661977236758134f;  // atan(t) / (pi/2)
     return swap ? 1.0f - a : a;
 }
@@ -513,9 +517,6 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                 if (pix < 0 || pix >= hs.npix) {
                     record(err, kCheckSkyIndex);
                 } else {
-                    // the action's per-pixel data (the sky) is requested now, so
-                    // its latency overlaps the geometry below
-                    const auto pre = act.fetch(pix);
                     const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
                     const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
                     const float dl = fmaf((float)kk, R0.y, R0.x);
@@ -569,7 +570,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                             const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
                             const float er = fmaf(wr, wr, -wi * wi) * iw;
                             const float ei = 2.0f * wr * wi * iw;
-                            act.pair(pix, pre, B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
+                            act.pair(pix, act.fetch(pix), B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
                                      fmaf(ei, F.c2p, er * F.s2p));
                         }
                     }
