@@ -168,13 +168,17 @@ def raster_scan(n: int = 20000):
 
 
 def sweep_scan(n: int, config_id: int, dec0: float = -80.0, ddec: float = 0.05,
-               per_sweep: int = 4096, stream: int = 1):
+               per_sweep: int = 4096, stream: int = 1, shard: int = 0, nshards: int = 1):
     """Constant-elevation sweep: RA advances 360 deg per `per_sweep` samples,
-    Dec steps `ddec` deg per sweep from `dec0`; psi uniform in [0, 180) deg."""
+    Dec steps `ddec` deg per sweep from `dec0`; psi uniform in [0, 180) deg.
+
+    shard / nshards: one of nshards interleaved parts of a sweep nshards times
+    as dense (shard k is offset by k / nshards of a sample in RA and draws its
+    own psi); shard 0 of 1 is the plain sweep."""
     i = np.arange(n, dtype=np.int64)
-    ra = 360.0 * (i % per_sweep) / per_sweep
+    ra = 360.0 * ((i % per_sweep) + shard / nshards) / per_sweep
     dec = dec0 + ddec * (i // per_sweep)
-    psi = rng_for(config_id, stream).uniform(0.0, 180.0, n)
+    psi = rng_for(config_id, stream + 1000 * shard).uniform(0.0, 180.0, n)
     return np.deg2rad(ra), np.deg2rad(dec), np.deg2rad(psi)
 
 

@@ -259,3 +259,51 @@ def test_edge_pointings(gpu, oracle_mod):
                                          pb_.astype(np.float64))
         np.testing.assert_allclose(a, oa, rtol=0, atol=1e-12 * max(1.0, np.abs(oa).max()))
         np.testing.assert_allclose(b, ob, rtol=0, atol=1e-12 * max(1.0, np.abs(ob).max()))
+
+
+def test_largest_sky_and_beam(gpu, oracle_mod):
+    """nside 8192 sky (805M pixels, the ring table at its largest) and an
+    nside 8192 beam: the TUNED disc equals the exact one, TUNED agrees with
+    the FP64 form, and per-sample disc sizes match the oracle's query_disc."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam
+
+    nss = nsb = 8192
+    npix = 12 * nss * nss
+    g = torch.Generator(device="cuda").manual_seed(5)
+    sky = torch.randn((npix, 4), generator=g, device="cuda", dtype=torch.float32)
+    sky[:, 3] = 0.0
+    rdeg = 0.1
+    npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(rdeg))
+    beam = PolBeam(nsb, npb, 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(0.04, 0.035, 30.0)
+    beam.build(nss)
+    rng = np.random.default_rng(31)
+    n = 400
+    ra = rng.uniform(0, 2 * np.pi, n)
+    dec = np.arcsin(rng.uniform(-1, 1, n))
+    dec[:20] = np.pi / 2 - rng.uniform(0, 0.004, 20)
+    dec[20:40] = -np.pi / 2 + rng.uniform(0, 0.004, 20)
+    pa = rng.uniform(0, np.pi, n)
+    t = [torch.tensor(x, device="cuda") for x in (ra, dec, pa)]
+    outs = {}
+    for form in ("tuned", "fp64"):
+        c = GPUConvolver(form=form)
+        c.set_sky_device(nss, sky.data_ptr(), False)
+        c.update_beam(beam)
+        c.set_scan_device(n, *[x.data_ptr() for x in t])
+        o = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(2)]
+        c.forward_device(o[0].data_ptr(), o[1].data_ptr(), out_f64=True)
+        c.sync()
+        outs[form] = [x.cpu().numpy() for x in o]
+        if form == "tuned":
+            worst, tp = c.tuned_calibrate(with_pairs=True)
+            pairs = c.count_pairs()
+            assert tp == pairs and worst < 0.5
+        c.close()
+    rho = oracle_mod.beam_rho_max(nsb, npb)
+    ref_pairs = sum(oracle_mod.query_disc(nss, np.pi / 2 - d, r, rho).size for r, d in zip(ra, dec))
+    assert pairs == ref_pairs
+    for k in range(2):
+        assert rel_max(outs["tuned"][k], outs["fp64"][k]) < 1e-6
