@@ -259,6 +259,20 @@ pisco_status pisco_adjoint(pisco_ctx* ctx, const void* g_a, const void* g_b, pis
                            void* gI, void* gQ, void* gU, void* gV, pisco_dtype out_dtype,
                            pisco_adjoint_mode mode);
 
+/* Beam-parameter gradient (the dbeam_params of the adjoint; no reference
+ * counterpart): dL/d(fwhm_deg, ellipticity, phi0_deg, dx, dy) of an
+ * elliptical Gaussian detector-pair beam (PolBeam's
+ * make_unpol_gaussian_elliptical_beams + build, polbeam.cpp:204-268, 290-372,
+ * with fwhm_x,y = F sqrt((1 +- e) / (1 -+ e)) and the centre offset by
+ * (dx, dy) radians in the beam plane), from gbeam = dL/dbeam (npix x 8 host
+ * doubles, a.IQUV b.IQUV, e.g. pisco_adjoint_device's d_gbeam).  The beam
+ * weights are recomputed and differentiated analytically, normalisation
+ * included. */
+pisco_status pisco_beam_gaussian_param_grad(int nside_beam, long npix, double epsilon,
+                                            int nside_sky, double fwhm_deg, double ellipticity,
+                                            double phi0_deg, double dx, double dy,
+                                            const double* gbeam, double grad[5]);
+
 /* ---- binned map-maker (replaces SkyMap, src/SkyMap/skymap.hpp:13-56) ---
  * Accumulates TOD into per-pixel normal equations (3 x 3 AtA and AtD, FP64,
  * device-resident) and solves them for I, Q, U.  Each pixel's totals

@@ -126,6 +126,7 @@ SIGNATURES = [
     ("pisco_beam_gaussian_fields", _S, [_I, _L, _D, _D, _D, _P, _P, _P, _P]),
     ("pisco_beam_from_fields", _S, [_L, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("pisco_beam_build", _S, [_I, _L, _D, ctypes.c_char, _I, _PP, _PP, _PP, _PP]),
+    ("pisco_beam_gaussian_param_grad", _S, [_I, _L, _D, _I, _D, _D, _D, _D, _D, _P, _P]),
     ("pisco_map_create", _S, [_I, _I, ctypes.POINTER(_P)]),
     ("pisco_map_destroy", None, [_P]),
     ("pisco_map_last_error", ctypes.c_char_p, [_P]),

@@ -29,7 +29,8 @@ from ._lib import (FLOAT32, FLOAT64, FORMS, PiscoError, PiscoInvalidArgument, Ru
                    check, load, ptr_array)
 
 __all__ = ["Scan", "Sky", "PolBeam", "Convolver", "GPUConvolver", "SkyMap", "RunConfig",
-           "PiscoError", "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix"]
+           "PiscoError", "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix",
+           "gaussian_beam_param_grad"]
 
 
 def _ptr(a: np.ndarray):
@@ -71,6 +72,23 @@ def beam_npix_for_radius(nside: int, radius_rad: float) -> int:
 
 
 # ------------------------------------------------------------------ API objects
+def gaussian_beam_param_grad(nside_beam: int, npix: int, epsilon: float, nside_sky: int,
+                             fwhm_deg: float, ellipticity: float, phi0_deg: float, dx: float,
+                             dy: float, gbeam) -> np.ndarray:
+    """dL/d(fwhm_deg, ellipticity, phi0_deg, dx, dy) of an elliptical Gaussian
+    pair beam from dL/dbeam (npix x 8), by pisco_beam_gaussian_param_grad."""
+    g = np.ascontiguousarray(gbeam, dtype=np.float64).reshape(-1)
+    if g.size != 8 * int(npix):
+        raise PiscoInvalidArgument(1, "gbeam must hold npix x 8 values")
+    out = np.zeros(5, np.float64)
+    check(load().pisco_beam_gaussian_param_grad(int(nside_beam), int(npix), float(epsilon),
+                                                int(nside_sky), float(fwhm_deg),
+                                                float(ellipticity), float(phi0_deg), float(dx),
+                                                float(dy), _ptr(g), _ptr(out)),
+          None, "gaussian_beam_param_grad")
+    return out
+
+
 class Scan:
     """Non-owning pointing view: ra, dec, pa arrays of length nsamples (radians)."""
 
