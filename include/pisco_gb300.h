@@ -273,6 +273,40 @@ pisco_status pisco_beam_gaussian_param_grad(int nside_beam, long npix, double ep
                                             double phi0_deg, double dx, double dy,
                                             const double* gbeam, double grad[5]);
 
+/* ---- beams built on the device (PolBeam construction, polbeam.cpp:117-372) --
+ * Outputs are d_ab = npix x 8 floats (a.I,Q,U,V, b.I,Q,U,V; device, 16-B
+ * aligned), the layout pisco_set_beam_device takes; set_beam != 0 also makes
+ * the result the context's beam.  Run on `stream` (NULL: the context's) and
+ * return without waiting.  Sums are deterministic (fixed order). */
+/* PolBeam::beam_from_fields for each enabled detector + PolBeam::build
+ * (polbeam.cpp:117-288): d_fields_a / d_fields_b = 4 x npix doubles (planes
+ * magEco, phsEco, magEcx, phsEcx; device); a detector's fields may be NULL when
+ * enabledDets leaves it out (its tilde beams are then zero).  Per pixel the
+ * host step's rounded operations; the normalisation is summed as a fixed tree
+ * and cos/sin are the device's, so results match pisco_beam_from_fields +
+ * pisco_beam_build to about one float ulp. */
+pisco_status pisco_beam_build_device(pisco_ctx* ctx, int nside_beam, long npix, double epsilon,
+                                     char enabledDets, int nside_sky, const double* d_fields_a,
+                                     const double* d_fields_b, float* d_ab, int set_beam,
+                                     void* stream);
+/* The beam of pisco_beam_gaussian_param_grad's model (elliptical Gaussian
+ * pair, fwhm_x,y = F sqrt((1 +- e) / (1 -+ e)), rotated by phi0, centre at
+ * (dx, dy) radians): a = b = ((1 + eps) g, (1 - eps) g, 0, 0) / N with
+ * N = (nside_sky / nside_beam)^2 sum g. */
+pisco_status pisco_beam_gaussian_device(pisco_ctx* ctx, int nside_beam, long npix, double epsilon,
+                                        int nside_sky, double fwhm_deg, double ellipticity,
+                                        double phi0_deg, double dx, double dy, float* d_ab,
+                                        int set_beam, void* stream);
+/* pisco_beam_gaussian_param_grad on the device: d_gbeam = dL/dbeam (npix x 8
+ * of g_dtype, device), d_grad = 5 device doubles dL/d(fwhm_deg, ellipticity,
+ * phi0_deg, dx, dy) (NaN when the model's weights sum to zero). */
+pisco_status pisco_beam_gaussian_param_grad_device(pisco_ctx* ctx, int nside_beam, long npix,
+                                                   double epsilon, int nside_sky, double fwhm_deg,
+                                                   double ellipticity, double phi0_deg, double dx,
+                                                   double dy, const void* d_gbeam,
+                                                   pisco_dtype g_dtype, double* d_grad,
+                                                   void* stream);
+
 /* ---- binned map-maker (replaces SkyMap, src/SkyMap/skymap.hpp:13-56) ---
  * Accumulates TOD into per-pixel normal equations (3 x 3 AtA and AtD, FP64,
  * device-resident) and solves them for I, Q, U.  Each pixel's totals

@@ -127,6 +127,10 @@ SIGNATURES = [
     ("pisco_beam_from_fields", _S, [_L, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("pisco_beam_build", _S, [_I, _L, _D, ctypes.c_char, _I, _PP, _PP, _PP, _PP]),
     ("pisco_beam_gaussian_param_grad", _S, [_I, _L, _D, _I, _D, _D, _D, _D, _D, _P, _P]),
+    ("pisco_beam_build_device", _S, [_P, _I, _L, _D, ctypes.c_char, _I, _P, _P, _P, _I, _P]),
+    ("pisco_beam_gaussian_device", _S, [_P, _I, _L, _D, _I, _D, _D, _D, _D, _D, _P, _I, _P]),
+    ("pisco_beam_gaussian_param_grad_device", _S,
+     [_P, _I, _L, _D, _I, _D, _D, _D, _D, _D, _P, _I, _P, _P]),
     ("pisco_map_create", _S, [_I, _I, ctypes.POINTER(_P)]),
     ("pisco_map_destroy", None, [_P]),
     ("pisco_map_last_error", ctypes.c_char_p, [_P]),

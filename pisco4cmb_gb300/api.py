@@ -336,6 +336,43 @@ class GPUConvolver:
                                            FLOAT64 if f64 else FLOAT32, stream or None),
               self.ctx, "set_beam_device")
 
+    def build_beam_device(self, nside: int, npix: int, epsilon: float, enabledDets: str,
+                          nside_sky: int, d_fields_a: int, d_fields_b: int, d_ab: int,
+                          set_beam: bool = True, stream: int = 0) -> None:
+        """PolBeam::beam_from_fields + build on the GPU: d_fields_* = 4 x npix
+        device doubles (magEco, phsEco, magEcx, phsEcx), d_ab = npix x 8
+        device floats out (a.IQUV, b.IQUV); set_beam makes it this
+        convolver's beam."""
+        check(load().pisco_beam_build_device(self.ctx, int(nside), int(npix), float(epsilon),
+                                             enabledDets.encode(), int(nside_sky),
+                                             d_fields_a or None, d_fields_b or None, d_ab,
+                                             1 if set_beam else 0, stream or None),
+              self.ctx, "build_beam_device")
+
+    def gaussian_beam_device(self, nside: int, npix: int, epsilon: float, nside_sky: int,
+                             fwhm_deg: float, ellipticity: float, phi0_deg: float, dx: float,
+                             dy: float, d_ab: int, set_beam: bool = True, stream: int = 0) -> None:
+        """The elliptical Gaussian pair beam of gaussian_beam_param_grad's
+        model, built on the GPU into d_ab (npix x 8 device floats)."""
+        check(load().pisco_beam_gaussian_device(self.ctx, int(nside), int(npix), float(epsilon),
+                                                int(nside_sky), float(fwhm_deg),
+                                                float(ellipticity), float(phi0_deg), float(dx),
+                                                float(dy), d_ab, 1 if set_beam else 0,
+                                                stream or None),
+              self.ctx, "gaussian_beam_device")
+
+    def gaussian_beam_param_grad_device(self, nside: int, npix: int, epsilon: float,
+                                        nside_sky: int, fwhm_deg: float, ellipticity: float,
+                                        phi0_deg: float, dx: float, dy: float, d_gbeam: int,
+                                        g_f64: bool, d_grad: int, stream: int = 0) -> None:
+        """dL/d(fwhm_deg, ellipticity, phi0_deg, dx, dy) into d_grad (5 device
+        doubles) from d_gbeam = dL/dbeam (npix x 8 device values)."""
+        check(load().pisco_beam_gaussian_param_grad_device(
+            self.ctx, int(nside), int(npix), float(epsilon), int(nside_sky), float(fwhm_deg),
+            float(ellipticity), float(phi0_deg), float(dx), float(dy), d_gbeam,
+            FLOAT64 if g_f64 else FLOAT32, d_grad, stream or None),
+            self.ctx, "gaussian_beam_param_grad_device")
+
     def adjoint_device(self, d_ga: int, d_gb: int, g_f64: bool, d_gsky: int, d_gbeam: int,
                        out_f64: bool = False, deterministic: bool = True, begin: int = 0,
                        n: int | None = None, stream: int = 0, sky_iqu: bool = False) -> None:

@@ -9,7 +9,11 @@ elliptical Gaussian beam with torch operations (the arithmetic of
 186-288, 290-372), with a pointing offset (dx, dy) of the beam centre, so
 that gradients with respect to FWHM, ellipticity and pointing offset follow
 by recomputing the beam weights: dL/dparam = sum_b dL/dbeam_b dbeam_b/dparam.
-No per-pair weights are stored.
+No per-pair weights are stored.  ``gaussian_beam`` is the same model as a
+``torch.autograd.Function`` on the library's kernels (beam built on the GPU
+by ``pisco_beam_gaussian_device``, gradient reduced by
+``pisco_beam_gaussian_param_grad_device``), for fitting loops that should not
+run the beam through torch operations.
 """
 from __future__ import annotations
 
@@ -20,7 +24,16 @@ import torch
 
 from .api import GPUConvolver, pix2ang
 
-__all__ = ["convolve", "gaussian_polbeam", "beam_pixel_coords", "ConvolveFn"]
+__all__ = ["convolve", "gaussian_polbeam", "gaussian_beam", "beam_pixel_coords", "ConvolveFn",
+           "GaussianBeamFn"]
+
+
+def _torch_stream(device=None) -> int:
+    """Handle of torch's current stream for the C ABI.  torch reports its
+    default (legacy) stream as 0, which the C ABI would take as "the
+    context's own stream" (non-blocking, unordered with torch's work), so it
+    is passed as cudaStreamLegacy (1) instead."""
+    return torch.cuda.current_stream(device).cuda_stream or 1
 
 
 class ConvolveFn(torch.autograd.Function):
@@ -33,7 +46,7 @@ class ConvolveFn(torch.autograd.Function):
             raise ValueError("sky and beam must be CUDA tensors")
         sky4 = _as_iquv(sky)
         bab = beam_ab.detach().to(torch.float32).contiguous()
-        stream = torch.cuda.current_stream().cuda_stream
+        stream = _torch_stream()
         conv.set_sky_device(nside_sky, sky4.data_ptr(), False, stream=stream)
         conv.set_beam_device(nside_beam, bab.shape[0], bab.data_ptr(), False, stream=stream)
         n = conv._n
@@ -52,7 +65,7 @@ class ConvolveFn(torch.autograd.Function):
         sky4, bab = ctx.saved_tensors
         conv = ctx.conv
         nside_sky, nside_beam, det, sky_shape, sky_dtype, beam_dtype = ctx.meta
-        stream = torch.cuda.current_stream().cuda_stream
+        stream = _torch_stream()
         # the context may have been reused since the forward: restore its inputs
         conv.set_sky_device(nside_sky, sky4.data_ptr(), False, stream=stream)
         conv.set_beam_device(nside_beam, bab.shape[0], bab.data_ptr(), False, stream=stream)
@@ -143,3 +156,43 @@ def gaussian_polbeam(rho, sigma, fwhm_deg, ellipticity, phi0_deg=0.0, dx=0.0, dy
     z = torch.zeros_like(g)
     a = torch.stack([(1 + epsilon) * g, (1 - epsilon) * g, z, z], dim=1) / norm
     return torch.cat([a, a], dim=1)
+
+
+class GaussianBeamFn(torch.autograd.Function):
+    """beam_ab (npixB x 8 float32, a.IQUV b.IQUV) of the elliptical Gaussian
+    pair model from params = (fwhm_deg, ellipticity, phi0_deg, dx, dy)."""
+
+    @staticmethod
+    def forward(ctx, params, conv: GPUConvolver, nside_beam: int, npix: int, epsilon: float,
+                nside_sky: int):
+        if params.numel() != 5:
+            raise ValueError("params must hold (fwhm_deg, ellipticity, phi0_deg, dx, dy)")
+        p = [float(v) for v in params.detach().double().cpu().tolist()]
+        dev = torch.device("cuda", conv.cfg.deviceId)
+        out = torch.empty((int(npix), 8), dtype=torch.float32, device=dev)
+        stream = _torch_stream(dev)
+        conv.gaussian_beam_device(nside_beam, npix, epsilon, nside_sky, *p, out.data_ptr(),
+                                  set_beam=False, stream=stream)
+        ctx.conv = conv
+        ctx.meta = (nside_beam, npix, epsilon, nside_sky, p, params.dtype, params.device, dev)
+        return out
+
+    @staticmethod
+    def backward(ctx, gbeam):
+        nside_beam, npix, epsilon, nside_sky, p, dtype, pdev, dev = ctx.meta
+        g = gbeam.to(dev)
+        if g.dtype not in (torch.float32, torch.float64):
+            g = g.to(torch.float64)
+        g = g.contiguous()
+        out = torch.empty(5, dtype=torch.float64, device=dev)
+        stream = _torch_stream(dev)
+        ctx.conv.gaussian_beam_param_grad_device(nside_beam, npix, epsilon, nside_sky, *p,
+                                                 g.data_ptr(), g.dtype == torch.float64,
+                                                 out.data_ptr(), stream=stream)
+        return out.to(device=pdev, dtype=dtype), None, None, None, None, None
+
+
+def gaussian_beam(params: torch.Tensor, conv: GPUConvolver, nside_beam: int, npix: int,
+                  epsilon: float = 0.01, nside_sky: int = 1) -> torch.Tensor:
+    """Differentiable Gaussian pair beam built by the library's kernels."""
+    return GaussianBeamFn.apply(params, conv, nside_beam, npix, epsilon, nside_sky)

@@ -7,6 +7,7 @@
 #include <complex>
 
 #include "../../include/pisco_gb300.h"
+#include "beam_model.h"
 #include "hpx.cuh"
 
 using namespace pisco;
@@ -131,15 +132,10 @@ pisco_status pisco_beam_build(int nside_beam, long npix, double eps, char en, in
     return PISCO_OK;
 }
 
-// Gradient of a loss with respect to the parameters of an elliptical Gaussian
-// detector-pair beam, from its gradient with respect to the beam maps.  The
-// beam (both detectors alike) is B[p] = c g[p] / N with c = (1 + eps,
-// 1 - eps, 0, 0) per detector, g = exp(-(ca x^2 + 2 cb x y + cc y^2)),
-// x = rho cos sigma - dx, y = rho sin sigma - dy at the pixel centres, and
-// N = (nside_sky / nside_beam)^2 sum_p g[p] (the PolBeam build normalisation,
-// polbeam.cpp:204-268); ca, cb, cc from sigma_x,y = fwhm_x,y / 2.35482 and
-// phi0, fwhm_x = F sqrt((1+e)/(1-e)), fwhm_y = F sqrt((1-e)/(1+e)).  The beam
-// weights are recomputed here (not stored); the derivative is analytic:
+// Gradient of a loss with respect to the parameters of the elliptical Gaussian
+// detector-pair beam model (beam_model.h), from its gradient with respect to
+// the beam maps.  The beam weights are recomputed here (not stored); the
+// derivative is analytic:
 //   dL/dt = (1/N) [sum_p G_p dg_p/dt - (sum_p G_p g_p) (sum_p dg_p/dt) / sum_p g_p],
 //   G_p = sum_k c_k dL/dB[p][k],  dg/dt = -g dQ/dt.
 pisco_status pisco_beam_gaussian_param_grad(int nside_beam, long npix, double eps, int nside_sky,
@@ -152,28 +148,10 @@ pisco_status pisco_beam_gaussian_param_grad(int nside_beam, long npix, double ep
         return PISCO_ERR_INVALID_ARGUMENT;
     if (npix > 12L * nside_beam * nside_beam) return PISCO_ERR_INVALID_ARGUMENT;
     const Hpx h = hpx_make(nside_beam);
-    const double d2r = kPi / 180.0, e = ellipticity;
-    const double fx = fwhm_deg * std::sqrt((1.0 + e) / (1.0 - e));
-    const double fy = fwhm_deg * std::sqrt((1.0 - e) / (1.0 + e));
-    const double sx = d2r * fx / 2.35482, sy = d2r * fy / 2.35482;
-    const double ph = d2r * phi0_deg;
-    const double c = std::cos(ph), s = std::sin(ph), s2 = std::sin(2.0 * ph), c2 = std::cos(2.0 * ph);
-    const double ux = 1.0 / (2.0 * sx * sx), uy = 1.0 / (2.0 * sy * sy);
-    const double ca = c * c * ux + s * s * uy;
-    const double cb = 0.5 * s2 * (uy - ux);
-    const double cc = s * s * ux + c * c * uy;
-    // derivatives of (ux, uy) with respect to F and e, of (ca, cb, cc) w.r.t. phi0
-    const double dux_dF = -2.0 * ux / fwhm_deg, duy_dF = -2.0 * uy / fwhm_deg;
-    const double dux_de = -2.0 * ux / (1.0 - e * e), duy_de = 2.0 * uy / (1.0 - e * e);
-    auto dcoef = [&](double dux, double duy, double& dca, double& dcb, double& dcc) {
-        dca = c * c * dux + s * s * duy;
-        dcb = 0.5 * s2 * (duy - dux);
-        dcc = s * s * dux + c * c * duy;
-    };
-    double aF, bF, cF, ae, be, ce;
-    dcoef(dux_dF, duy_dF, aF, bF, cF);
-    dcoef(dux_de, duy_de, ae, be, ce);
-    const double ap = d2r * s2 * (uy - ux), bp = d2r * c2 * (uy - ux), cp = d2r * s2 * (ux - uy);
+    const GaussModel m = gauss_model(fwhm_deg, ellipticity, phi0_deg);
+    const double ca = m.ca, cb = m.cb, cc = m.cc;
+    const double aF = m.aF, bF = m.bF, cF = m.cF, ae = m.ae, be = m.be, ce = m.ce;
+    const double ap = m.ap, bp = m.bp, cp = m.cp;
     const double cw[8] = {1.0 + eps, 1.0 - eps, 0.0, 0.0, 1.0 + eps, 1.0 - eps, 0.0, 0.0};
     double sg = 0.0, sGg = 0.0, sdg[5] = {0, 0, 0, 0, 0}, sGdg[5] = {0, 0, 0, 0, 0};
     for (long p = 0; p < npix; ++p) {

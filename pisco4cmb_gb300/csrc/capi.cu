@@ -65,7 +65,7 @@ pisco_ctx::~pisco_ctx()
     for (void* p : {(void*)d_dets, (void*)d_items, (void*)d_queue, (void*)adj_sky32,
                     (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red,
                     (void*)rings, (void*)ord, (void*)ord_keys, (void*)ord_keys2,
-                    (void*)ord_pos, ord_tmp})
+                    (void*)ord_pos, ord_tmp, (void*)beam_scr})
         if (p) cudaFree(p);
     for (int* p : det_ord)
         if (p) cudaFree(p);

@@ -113,6 +113,10 @@ struct pisco_ctx {
     double* red = nullptr;
     size_t red_cap = 0;
 
+    // device beam construction scratch (block partials, results, weights)
+    double* beam_scr = nullptr;
+    size_t beam_scr_cap = 0;
+
     ~pisco_ctx();
     pisco_status activate();
     pisco_status ensure(void** p, size_t* cap, size_t bytes, const char* what);
