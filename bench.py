@@ -801,6 +801,90 @@ def run_map_study(args):
     return 0
 
 
+def run_beam_study(args):
+    """Beam construction on the GPU against the host PolBeam builder, for the
+    c2 beam (nside 2048, 3 deg, FWHM 1.5 deg, e 0.05; sky nside 1024), the c3
+    beam (nside 4096, 1 deg, FWHM 0.5 deg, e 0.02; sky 2048) and a wide one
+    (nside 8192, 5 deg, FWHM 2 deg, e 0.05; sky 2048).  Per case: the host
+    builder (make_unpol_gaussian_elliptical_beams + build, one thread), the
+    device build from field planes (pisco_beam_build_device; 64 B of fields
+    in + 32 B of beam out per pixel), the device Gaussian model and its
+    parameter gradient (32 B of gbeam in per pixel), and the largest float ulp
+    difference between the device and host builds."""
+    import ctypes
+
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, beam_npix_for_radius, synth
+    from pisco4cmb_gb300._lib import check, load
+
+    cs = _study_stream()
+    conv = GPUConvolver(form="tuned")
+    conv.configure_execution()
+    e0, e1 = _events()
+    hbm_peak, peak_kind = measured_peaks()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(max(args.steps, 5)):
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts)) / 1e3
+
+    for name, nsb, rdeg, fwhm, ell, nss in (("c2_beam", 2048, 3.0, 1.5, 0.05, 1024),
+                                             ("c3_beam", 4096, 1.0, 0.5, 0.02, 2048),
+                                             ("wide_beam", 8192, 5.0, 2.0, 0.05, 2048)):
+        npix = beam_npix_for_radius(nsb, math.radians(rdeg))
+        fx, fy = synth.elliptical_fwhm(fwhm, ell)
+        t0 = time.perf_counter()
+        hb = PolBeam(nsb, npix, 0.01, "p")
+        hb.make_unpol_gaussian_elliptical_beams(fx, fy, 0.0)
+        hb.build(nss)
+        t_host = time.perf_counter() - t0
+        f = [np.empty(npix, np.float64) for _ in range(4)]
+        check(load().pisco_beam_gaussian_fields(nsb, npix, fx, fy, 0.0,
+                                                *[x.ctypes.data_as(ctypes.c_void_p) for x in f]))
+        fd = torch.tensor(np.stack(f), device="cuda")
+        out = torch.empty((npix, 8), dtype=torch.float32, device="cuda")
+        gb = torch.randn((npix, 8), dtype=torch.float32, device="cuda")
+        grad = torch.empty(5, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t_build = timed(lambda: conv.build_beam_device(nsb, npix, 0.01, "p", nss, fd.data_ptr(),
+                                                       fd.data_ptr(), out.data_ptr(),
+                                                       set_beam=False, stream=cs))
+        a, b = hb.planes()
+        host = np.concatenate([a.T, b.T], axis=1)
+        dev = out.cpu().numpy()
+        hi = host.view(np.int32).astype(np.int64)
+        di = dev.view(np.int32).astype(np.int64)
+        ulp = int(np.abs(np.where(hi < 0, -(hi & 0x7FFFFFFF), hi) -
+                         np.where(di < 0, -(di & 0x7FFFFFFF), di)).max())
+        t_model = timed(lambda: conv.gaussian_beam_device(nsb, npix, 0.01, nss, fwhm, ell, 0.0,
+                                                          0.0, 0.0, out.data_ptr(),
+                                                          set_beam=False, stream=cs))
+        t_grad = timed(lambda: conv.gaussian_beam_param_grad_device(
+            nsb, npix, 0.01, nss, fwhm, ell, 0.0, 0.0, 0.0, gb.data_ptr(), False,
+            grad.data_ptr(), stream=cs))
+        line = {"workload": "beam_" + name, "beam_pixels": npix, "nside_beam": nsb,
+                "radius_deg": rdeg, "host_build_ms": t_host * 1e3,
+                "device_build_ms": t_build * 1e3,
+                "device_build_gbs": 96.0 * npix / t_build / 1e9,
+                "device_model_ms": t_model * 1e3, "device_param_grad_ms": t_grad * 1e3,
+                "device_param_grad_gbs": 32.0 * npix / t_grad / 1e9,
+                "hbm_peak_gbs": hbm_peak, "peak": peak_kind,
+                "max_ulp_device_vs_host": ulp,
+                "cpu_baseline": {"kind": "port", "cores": 1,
+                                 "sample": "whole beam, library host builder "
+                                           "(bit-identical to the reference PolBeam)"}}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -812,7 +896,7 @@ def main():
     ap.add_argument("--accuracy-samples", type=int, default=50_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map", "beam"],
                     help="c2 = the headline line; the others print their own study lines")
     ap.add_argument("--fp64-samples", type=int, default=200_000)
     ap.add_argument("--cpu-samples", type=int, default=2_000)
@@ -830,7 +914,8 @@ def main():
         if args.samples == 2_000_000:
             args.samples = 0  # the workload's own sample count
         return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint,
-                "order": run_order_study, "map": run_map_study}[args.workload](args)
+                "order": run_order_study, "map": run_map_study,
+                "beam": run_beam_study}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 
