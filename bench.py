@@ -885,6 +885,62 @@ def run_beam_study(args):
     return 0
 
 
+def run_refgpu_study(args):
+    """The reference's own GPU pipeline on this GB300: its kernels K1 + K2
+    (cudaConv2.cu, compiled unmodified for sm_103a) with GPUConvolver's host
+    orchestration (query_disc on all host cores, ptgPerConv = 2048 chunks,
+    per-chunk copies; oracle/ref_gpu_harness.cpp), on the first
+    --samples (default 65,536) samples of the c2 workload, beside this
+    library's TUNED forward on the same samples through the same host-array
+    call (exec_convolution: host pointing in, host TOD out)."""
+    import oracle
+    from pisco4cmb_gb300 import GPUConvolver, Scan, Sky
+
+    if not oracle.refgpu_available():
+        print(json.dumps({"workload": "refgpu_c2", "unavailable":
+                          "reference GPU kernels not built (needs the reference tree at build time)"}))
+        return 0
+    n = args.samples or 65536
+    n -= n % 2048
+    wl = make_workload("cuda", n)
+    sky = np.asarray(wl["sky"], np.float32)
+    ba, bb = wl["beam"].planes()
+    ra, dec, pa = (np.asarray(wl[k][:n], np.float32) for k in ("ra", "dec", "pa"))
+    cores = host_cores()
+    # pixPerDisc as a caller of the reference would set it: the largest disc of the sample
+    ra_, rb_, t = oracle.refgpu_convolve(ra, dec, pa, wl["nside_sky"], sky, wl["beam"].nside,
+                                         ba, bb, nthreads=cores)
+    conv = GPUConvolver(form="tuned")
+    conv.update_sky(Sky(wl["nside_sky"], sky[0], sky[1], sky[2], None))
+    conv.update_beam(wl["beam"])
+    conv.update_scan(Scan(n, ra, dec, pa))
+    a = np.zeros(n, np.float32)
+    b = np.zeros(n, np.float32)
+    conv.exec_convolution(a, b)  # warm-up
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        conv.exec_convolution(a, b)
+        ts.append(time.perf_counter() - t0)
+    t_ours = float(np.median(ts))
+    rms = float(np.sqrt(np.mean(a.astype(np.float64) ** 2)))
+    d = np.concatenate([a - ra_, b - rb_]).astype(np.float64)
+    line = {"workload": "refgpu_c2", "samples": int(n), "host_cores": cores,
+            "reference_gpu": {"samples_per_s": n / t[0], "kernel_samples_per_s": n / t[1],
+                              "total_s": t[0], "kernels_s": t[1], "query_disc_s": t[2],
+                              "copies_s": t[3],
+                              "kind": "reference K1+K2 recompiled for sm_103a, GPUConvolver "
+                                      "orchestration, query_disc restated"},
+            "tuned_host_api": {"samples_per_s": n / t_ours, "seconds": t_ours},
+            "speedup_vs_reference_gpu": t[0] / t_ours,
+            "speedup_vs_reference_kernels": t[1] / t_ours,
+            "rms_diff_over_tod_rms": float(np.sqrt(np.mean(d ** 2))) / rms,
+            "max_diff_over_tod_rms": float(np.abs(d).max()) / rms}
+    print(json.dumps(line), flush=True)
+    conv.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -896,7 +952,8 @@ def main():
     ap.add_argument("--accuracy-samples", type=int, default=50_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map", "beam"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map", "beam",
+                             "refgpu"],
                     help="c2 = the headline line; the others print their own study lines")
     ap.add_argument("--fp64-samples", type=int, default=200_000)
     ap.add_argument("--cpu-samples", type=int, default=2_000)
@@ -915,7 +972,7 @@ def main():
             args.samples = 0  # the workload's own sample count
         return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint,
                 "order": run_order_study, "map": run_map_study,
-                "beam": run_beam_study}[args.workload](args)
+                "beam": run_beam_study, "refgpu": run_refgpu_study}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 

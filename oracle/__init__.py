@@ -21,6 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpisco_ref.so")
 REFDEV_LIB = os.path.join(HERE, "_ref", "libpisco_refdev.so")
+REFGPU_CUBIN = os.path.join(HERE, "_ref", "refconv.cubin")
+REFGPU_LIB = os.path.join(HERE, "librefgpu.so")
 
 _i64 = ctypes.c_int64
 _dbl = ctypes.c_double
@@ -39,6 +41,69 @@ def build_oracle(force: bool = False) -> str:
                            "-std=c99", src, "-o", tmp, "-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+def build_refgpu(force: bool = False):
+    """Compile the harness that runs the reference's GPU kernels
+    (ref_gpu_harness.cpp + oracle.c, CUDA driver API) into librefgpu.so;
+    None when the CUDA headers are missing."""
+    srcs = [os.path.join(HERE, f) for f in ("ref_gpu_harness.cpp", "oracle.c", "oracle.h")]
+    if (not force and os.path.exists(REFGPU_LIB)
+            and all(os.path.getmtime(REFGPU_LIB) >= os.path.getmtime(f) for f in srcs)):
+        return REFGPU_LIB
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if not os.path.exists(os.path.join(cuda, "include", "cuda.h")):
+        return None
+    obj = REFGPU_LIB + ".oracle%d.o" % os.getpid()
+    tmp = REFGPU_LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c99",
+                           "-c", srcs[1], "-o", obj])
+    subprocess.check_call(["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                           "-I", os.path.join(cuda, "include"), "-I", HERE, srcs[0], obj,
+                           "-L", os.path.join(cuda, "lib64", "stubs"), "-lcuda", "-o", tmp])
+    os.remove(obj)
+    os.replace(tmp, REFGPU_LIB)
+    return REFGPU_LIB
+
+
+def refgpu_available() -> bool:
+    """The reference-kernel cubin and the harness are both built."""
+    return os.path.exists(REFGPU_CUBIN) and os.path.exists(REFGPU_LIB)
+
+
+def refgpu_convolve(ra, dec, pa, nside_sky, sky, nside_beam, beam_a, beam_b,
+                    ptg_per_conv=2048, pix_per_disc=None, nthreads=0):
+    """The reference's GPU pipeline (its kernels K1 + K2 with GPUConvolver's
+    chunking) on float inputs; sky 3|4 x npix, beams 4 x npixB.  Returns
+    (tod_a, tod_b, times) for the first n - n % ptg_per_conv samples; times =
+    (total, kernels, query_disc, copies) in seconds."""
+    L = ctypes.CDLL(REFGPU_LIB)
+    L.refgpu_convolve.restype = ctypes.c_long
+    L.refgpu_last_error.restype = ctypes.c_char_p
+    ra, dec, pa = (_c(x, np.float32) for x in (ra, dec, pa))
+    sky = _c(sky, np.float32)
+    if sky.shape[0] == 3:
+        sky = np.concatenate([sky, np.zeros((1, sky.shape[1]), np.float32)])
+    sky4 = np.ascontiguousarray(sky.T)
+    ba = np.ascontiguousarray(_c(beam_a, np.float32).T)
+    bb = np.ascontiguousarray(_c(beam_b, np.float32).T)
+    n = ra.size
+    if pix_per_disc is None:
+        rho = beam_rho_max(nside_beam, ba.shape[0])
+        pix_per_disc = max(int(lib().orc_query_disc_count(nside_sky, float(np.pi / 2 - d),
+                                                          float(r), rho))
+                           for r, d in zip(ra.astype(np.float64), dec.astype(np.float64)))
+    oa = np.zeros(n, np.float32)
+    ob = np.zeros(n, np.float32)
+    t = np.zeros(4, np.float64)
+    done = L.refgpu_convolve(REFGPU_CUBIN.encode(), ctypes.c_int(nside_sky), _ptr(sky4),
+                             ctypes.c_int(nside_beam), ctypes.c_long(ba.shape[0]), _ptr(ba),
+                             _ptr(bb), ctypes.c_long(n), _ptr(ra), _ptr(dec), _ptr(pa),
+                             ctypes.c_int(ptg_per_conv), ctypes.c_int(int(pix_per_disc)),
+                             ctypes.c_int(nthreads), _ptr(oa), _ptr(ob), _ptr(t))
+    if done < 0:
+        raise RuntimeError("reference GPU pipeline: " + L.refgpu_last_error().decode())
+    return oa[:done], ob[:done], tuple(t)
 
 
 def build_ref() -> bool:

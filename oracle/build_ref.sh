@@ -13,6 +13,10 @@
 #   libpisco_refdev.so : the reference's device HEALPix port and device
 #                        rotation (cudaHealpix.cu, cudaSphtransf.cu)
 #                        compiled for the host with __device__ removed.
+#   refconv.cubin      : the reference's device code (cudaHealpix.cu,
+#                        cudaSphtransf.cu, cudaConv2.cu: kernels K1, K2)
+#                        compiled unmodified for sm_103a, loaded at run time
+#                        by oracle/ref_gpu_harness.cpp.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${PISCO_REFERENCE:-/root/reference}
@@ -51,4 +55,7 @@ g++ $DEVF -c "$REF/src/GpuConvolver/cuda/cudaSphtransf.cu" -o "$OUT/obj/cudaSpht
 g++ -O2 -fPIC -w -I$REF/src -I$CUDA_INC -D__device__= -c "$HERE/refdev_harness.cpp" -o "$OUT/obj/refdev_harness.o"
 g++ -shared -o "$OUT/libpisco_refdev.so" "$OUT"/obj/cudaHealpix.o "$OUT"/obj/cudaSphtransf.o \
     "$OUT"/obj/refdev_harness.o
-echo "build_ref.sh: built $OUT/libpisco_ref.so, libpisco_refmap*.so and libpisco_refdev.so"
+NVCC=${CUDA_HOME:-/usr/local/cuda}/bin/nvcc
+"$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -O3 -I"$REF/src/GpuConvolver/cuda" \
+    -o "$OUT/refconv.cubin" "$HERE/ref_gpu_kernels.cu"
+echo "build_ref.sh: built $OUT/libpisco_ref.so, libpisco_refmap*.so, libpisco_refdev.so and refconv.cubin"
