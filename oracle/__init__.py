@@ -89,10 +89,13 @@ def refgpu_convolve(ra, dec, pa, nside_sky, sky, nside_beam, beam_a, beam_b,
     bb = np.ascontiguousarray(_c(beam_b, np.float32).T)
     n = ra.size
     if pix_per_disc is None:
+        # the largest disc (over at most 50,000 evenly spaced samples, plus a
+        # 2 % margin beyond that many); the harness reports an overflow
         rho = beam_rho_max(nside_beam, ba.shape[0])
-        pix_per_disc = max(int(lib().orc_query_disc_count(nside_sky, float(np.pi / 2 - d),
-                                                          float(r), rho))
-                           for r, d in zip(ra.astype(np.float64), dec.astype(np.float64)))
+        idx = np.arange(n) if n <= 50_000 else np.linspace(0, n - 1, 50_000).astype(np.int64)
+        big = max(int(lib().orc_query_disc_count(nside_sky, float(np.pi / 2 - float(dec[i])),
+                                                 float(ra[i]), rho)) for i in idx)
+        pix_per_disc = big if n <= 50_000 else int(big * 1.02) + 64
     oa = np.zeros(n, np.float32)
     ob = np.zeros(n, np.float32)
     t = np.zeros(4, np.float64)
