@@ -405,6 +405,8 @@ def run_gpu_arm(args, rank, world, local):
             "clocks": clk.summary(),
             "input_gen_s": wl["gen_s"],
         }
+        if not args.no_cpu:
+            line["reference_gpu"] = reference_gpu_sample(wl, 16384)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -883,6 +885,28 @@ def run_beam_study(args):
                                            "(bit-identical to the reference PolBeam)"}}
         print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_gpu_sample(wl, m: int):
+    """The reference's own GPU pipeline (K1 + K2 recompiled for sm_103a) on the
+    first m samples of the workload, or why it did not run."""
+    import oracle
+
+    if not oracle.refgpu_available():
+        return {"unavailable": "reference GPU kernels not built (needs the reference tree at "
+                               "build time)"}
+    try:
+        m -= m % 2048
+        ba, bb = wl["beam"].planes()
+        ra, dec, pa = (np.asarray(wl[k][:m], np.float32) for k in ("ra", "dec", "pa"))
+        _, _, t = oracle.refgpu_convolve(ra, dec, pa, wl["nside_sky"],
+                                         np.asarray(wl["sky"], np.float32), wl["beam"].nside,
+                                         ba, bb, nthreads=host_cores())
+    except Exception as e:  # noqa: BLE001  (a baseline must not break the headline line)
+        return {"unavailable": str(e)[:200]}
+    return {"value": m / t[0], "unit": "samples/s", "kernels_only": m / t[1],
+            "sample": "first %d samples" % m,
+            "kind": "reference K1+K2 recompiled for sm_103a with GPUConvolver's pipeline"}
 
 
 def run_refgpu_study(args):
