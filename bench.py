@@ -892,6 +892,68 @@ def run_beam_study(args):
     return 0
 
 
+def run_bilinear_study(args):
+    """Bilinear beam lookup (HEALPix get_interpol, the reference's
+    commented-out convolver.cpp:162-185 path) on the c2 workload: TUNED with
+    the FP32 stencil over all samples against TUNED nearest, PLAIN bilinear on
+    a bounded prefix, and the error against the FP64 form's bilinear lookup on
+    that prefix (relative to the TOD rms)."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, Sky
+
+    n = args.samples or 2_000_000
+    wl = make_workload("cuda", n)
+    sky = np.asarray(wl["sky"], np.float32)
+    cs = _study_stream()
+    e0, e1 = _events()
+    t = [torch.tensor(np.asarray(wl[k][:n], np.float64), device="cuda") for k in ("ra", "dec", "pa")]
+    torch.cuda.synchronize()
+
+    def conv(form, interp, m, f64=False):
+        c = GPUConvolver(form=form)
+        planes = [sky[k].astype(np.float64) if f64 else sky[k] for k in range(3)]
+        c.update_sky(Sky(wl["nside_sky"], planes[0], planes[1], planes[2], None))
+        c.update_beam(wl["beam"])
+        c.set_interp(interp)
+        c.set_scan_device(m, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(), stream=cs)
+        return c
+
+    def timed(c, m, reps):
+        a = torch.empty(m, dtype=torch.float64, device="cuda")
+        b = torch.empty(m, dtype=torch.float64, device="cuda")
+        c.forward_device(a.data_ptr(), b.data_ptr(), out_f64=True, stream=cs)  # warm-up
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            c.forward_device(a.data_ptr(), b.data_ptr(), out_f64=True, stream=cs)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.median(ts)), a.cpu().numpy()
+
+    reps = max(3, min(args.steps, 5))
+    t_near, _ = timed(conv("tuned", False, n), n, reps)
+    t_bil, a_bil = timed(conv("tuned", True, n), n, reps)
+    m = min(n, args.plain_samples)
+    t_plain, _ = timed(conv("plain", True, m), m, 1)
+    k = min(n, args.fp64_samples)
+    _, a64 = timed(conv("fp64", True, k, f64=True), k, 1)
+    rms = float(np.sqrt(np.mean(a64 ** 2)))
+    d = a_bil[:k] - a64
+    line = {"workload": "bilinear_c2_nside1024_beam3deg", "nsamples": n,
+            "tuned_nearest": {"ms": t_near * 1e3, "samples_per_s": n / t_near},
+            "tuned_bilinear": {"ms": t_bil * 1e3, "samples_per_s": n / t_bil,
+                               "over_nearest": t_bil / t_near},
+            "plain_bilinear": {"samples_per_s": m / t_plain, "sample": m,
+                               "tuned_over_plain": (n / t_bil) / (m / t_plain)},
+            "tuned_bilinear_vs_fp64_bilinear": {"rms": float(np.sqrt(np.mean(d ** 2))) / rms,
+                                                "max": float(np.abs(d).max()) / rms,
+                                                "sample": k, "relative_to": "TOD rms"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def reference_gpu_sample(wl, m: int):
     """The reference's own GPU pipeline (K1 + K2 recompiled for sm_103a) on the
     first m samples of the workload, or why it did not run."""
@@ -982,7 +1044,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "order", "map", "beam",
-                             "refgpu"],
+                             "refgpu", "bilinear"],
                     help="c2 = the headline line; the others print their own study lines")
     ap.add_argument("--fp64-samples", type=int, default=200_000)
     ap.add_argument("--cpu-samples", type=int, default=2_000)
@@ -1001,7 +1063,8 @@ def main():
             args.samples = 0  # the workload's own sample count
         return {"c3": run_c3_precision, "c4": run_c4_batched, "c5": run_c5_adjoint,
                 "order": run_order_study, "map": run_map_study,
-                "beam": run_beam_study, "refgpu": run_refgpu_study}[args.workload](args)
+                "beam": run_beam_study, "refgpu": run_refgpu_study,
+                "bilinear": run_bilinear_study}[args.workload](args)
     return run_gpu_arm(args, rank, world, local)
 
 

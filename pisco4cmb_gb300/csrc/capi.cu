@@ -579,13 +579,13 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
         a.sky64 = c->sky64;
         a.beam64 = c->beam64;
         e = launch_forward_plain(a, true, c->sm_count, s);
-    } else if (form == PISCO_FORM_TUNED && c->interp == PISCO_BEAM_NEAREST &&
+    } else if (form == PISCO_FORM_TUNED &&
                tuned_supported(c->nside_beam, (int)c->npix_beam, c->rho_max)) {
         CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
         e = launch_forward_tuned(a, c->sm_count, s);
     } else {
-        // PLAIN, and TUNED outside the tuned geometry's domain (bilinear beam
-        // lookup or a beam reaching beyond the polar cap of its grid).
+        // PLAIN, and TUNED outside the tuned geometry's domain (a beam
+        // reaching beyond the polar cap of its grid).
         e = launch_forward_plain(a, false, c->sm_count, s);
     }
     if (a.order) c->order_used(s);

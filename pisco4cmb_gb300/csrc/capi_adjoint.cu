@@ -111,6 +111,9 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
 {
     if (!c) return PISCO_ERR_INVALID_ARGUMENT;
     if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
+    if (c->interp != PISCO_BEAM_NEAREST)
+        return fail(c, PISCO_ERR_UNSUPPORTED, "the adjoint is the transpose of the nearest-pixel "
+                                              "beam lookup; set PISCO_BEAM_NEAREST");
     if (begin < 0 || n < 0 || begin + n > c->nsamples)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sample range outside the scan");
     if (n > 0 && (!d_ga || !d_gb)) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "TOD gradients are NULL");
@@ -247,6 +250,9 @@ pisco_status pisco_adjoint(pisco_ctx* c, const void* g_a, const void* g_b, pisco
                            pisco_adjoint_mode mode)
 {
     if (!c) return PISCO_ERR_INVALID_ARGUMENT;
+    if (c->interp != PISCO_BEAM_NEAREST)
+        return fail(c, PISCO_ERR_UNSUPPORTED, "the adjoint is the transpose of the nearest-pixel "
+                                              "beam lookup; set PISCO_BEAM_NEAREST");
     if (g_dtype != PISCO_FLOAT32 && g_dtype != PISCO_FLOAT64) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
     if (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
     if (!c->nside_sky) return fail(c, PISCO_ERR_NOT_READY, "no sky set");

@@ -55,6 +55,9 @@ pisco_status validate(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "need 1..65536 detector descriptors");
     if (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad output dtype");
+    if (c->interp != PISCO_BEAM_NEAREST)
+        return fail(c, PISCO_ERR_UNSUPPORTED, "the batched launch uses the nearest-pixel beam "
+                                              "lookup; set PISCO_BEAM_NEAREST");
     if (!c->sky32 || !c->nside_sky) return fail(c, PISCO_ERR_NOT_READY, "no sky set");
     for (int d = 0; d < ndet; ++d) {
         const pisco_det_desc& x = dets[d];

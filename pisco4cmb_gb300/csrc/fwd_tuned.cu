@@ -16,7 +16,8 @@ namespace {
 
 constexpr int kTW = PISCO_TUNED_WARPS;
 
-template <bool kCalib>
+// kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
+template <bool kCalib, bool kBil>
 __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
     tuned_kernel(FwdArgs a, float rscale, float* calib)
 {
@@ -38,10 +39,10 @@ __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
         const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i
         const long long s = a.begin + j;
         const tuned::Out o{a.out_a, a.out_b, j, a.out_f64};
-        tuned::sample<kCalib>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane, a.err,
-                              g, nfall, cmax, npairs);
+        tuned::sample<kCalib, kBil>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane,
+                                    a.err, g, nfall, cmax, npairs);
     }
-    tuned::flush(hs, S, Q, lane, a.err, g);
+    tuned::flush<kBil>(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
     if (kCalib && calib) {
 #pragma unroll
@@ -93,12 +94,16 @@ cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, f
     const int threads = kTW * 32;
     const float rscale = (float)(1.7320508075688772 * (double)a.nside_beam);
     const long long need = (a.n + kTW - 1) / kTW;
+    // calibration measures the nearest-pixel decisions, whatever the lookup
     if (calib) {
-        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<true>, threads);
-        tuned_kernel<true><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, calib);
+        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<true, false>, threads);
+        tuned_kernel<true, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, calib);
+    } else if (a.interp == 1) {
+        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, true>, threads);
+        tuned_kernel<false, true><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, nullptr);
     } else {
-        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false>, threads);
-        tuned_kernel<false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, nullptr);
+        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, false>, threads);
+        tuned_kernel<false, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, nullptr);
     }
     return cudaGetLastError();
 }

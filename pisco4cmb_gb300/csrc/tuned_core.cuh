@@ -246,11 +246,119 @@ __device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan&
     return s;
 }
 
+// Bilinear beam value of the PLAIN form (HEALPix get_interpol in FP64; the
+// weights of stencil pixels outside the stored map are dropped and the rest
+// renormalised; the value rounded to float).  false: no stencil pixel lies in
+// the map.
+__device__ __forceinline__ bool bilinear_f64(const Hpx& hb, int npb, double rho, double sig,
+                                             const F8* beam, F8& out)
+{
+    int64_t px[4];
+    double w[4];
+    get_interpol(hb, rho, sig, px, w);
+    double ws = 0.0, va[4] = {0.0, 0.0, 0.0, 0.0}, vb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (px[i] < 0 || px[i] >= npb) continue;
+        ws += w[i];
+        const F8 B = beam[px[i]];
+        va[0] += B.a.x * w[i]; va[1] += B.a.y * w[i]; va[2] += B.a.z * w[i]; va[3] += B.a.w * w[i];
+        vb[0] += B.b.x * w[i]; vb[1] += B.b.y * w[i]; vb[2] += B.b.z * w[i]; vb[3] += B.b.w * w[i];
+    }
+    if (!(ws > 0.0)) return false;
+    out.a = make_float4((float)(va[0] / ws), (float)(va[1] / ws), (float)(va[2] / ws),
+                        (float)(va[3] / ws));
+    out.b = make_float4((float)(vb[0] / ws), (float)(vb[1] / ws), (float)(vb[2] / ws),
+                        (float)(vb[3] / ws));
+    return true;
+}
+
+// (f(a) - f(b)) / (2c (a - b)) for f(x) = 2 asin(c x), the colatitude of ring
+// height x (x = nside sqrt(3 (1 - cos theta)), c = 1 / (sqrt(6) nside)), by
+// the asin series to c^4 (relative truncation below 1e-8 for theta <= 0.5).
+__device__ __forceinline__ float asin_slope(float a, float b, float c2)
+{
+    const float s2 = fmaf(a, a, fmaf(a, b, b * b));
+    const float a2 = a * a, b2 = b * b;
+    const float s4 = fmaf(a2, a2, fmaf(a2, a * b, fmaf(a2, b2, fmaf(a * b, b2, b2 * b2))));
+    return fmaf(c2 * c2 * 0.075f, s4, fmaf(c2 * (1.0f / 6.0f), s2, 1.0f));
+}
+
+// The same stencil in FP32 from the pair's polar-cap coordinates on the beam
+// grid: r = nside sqrt(3 (1 - cos rho)) and sigma = (qd + tp) pi/2.  Rings of
+// the north cap: ring i holds 4i pixels from 2i(i - 1), half a pixel shifted;
+// get_interpol takes the ring above (floor r) and the next one, interpolates
+// in longitude on each and linearly in colatitude between them (ring 1 and
+// its image across the pole when r < 1).  The weights are continuous across
+// every floor decision, so FP32 index choices near a boundary change the
+// value only by the FP32 error of r and tp: no FP64 re-evaluation is needed.
+__device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, float r, F8& out)
+{
+    const float c = 1.0f / (2.4494897427831781f * (float)B.nside);  // 1 / (sqrt(6) nside)
+    const float c2 = c * c;
+    const int k = (int)r;  // ring above (0 above the first ring)
+    int px[4];
+    float w[4];
+    // longitude interpolation on ring i: pixels start + i1, start + i1 + 1
+    auto ring = [&](int i, int& p1, int& p2, float& w1, float& w2) {
+        const float t = fmaf(tp, (float)i, -0.5f);
+        const float fl = floorf(t);
+        const float f = t - fl;
+        int i1 = (int)fl + qd * i, i2 = i1 + 1;
+        const int np = 4 * i;
+        if (i1 < 0) i1 += np;
+        if (i2 >= np) i2 -= np;
+        const int start = 2 * i * (i - 1);
+        p1 = start + i1;
+        p2 = start + i2;
+        w1 = 1.0f - f;
+        w2 = f;
+    };
+    if (k == 0) {
+        ring(1, px[2], px[3], w[2], w[3]);
+        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
+        const float f = 0.25f * (1.0f - wt);
+        w[0] = f;
+        w[1] = f;
+        w[2] = fmaf(w[2], wt, f);
+        w[3] = fmaf(w[3], wt, f);
+        px[0] = (px[2] + 2) & 3;
+        px[1] = (px[3] + 2) & 3;
+    } else {
+        ring(k, px[0], px[1], w[0], w[1]);
+        ring(k + 1, px[2], px[3], w[2], w[3]);
+        const float kf = (float)k;
+        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
+        w[0] *= 1.0f - wt;
+        w[1] *= 1.0f - wt;
+        w[2] *= wt;
+        w[3] *= wt;
+    }
+    float ws = 0.0f;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (px[i] < 0 || px[i] >= B.npix) continue;
+        ws += w[i];
+        const F8 v = B.beam[px[i]];
+        a.x = fmaf(v.a.x, w[i], a.x); a.y = fmaf(v.a.y, w[i], a.y);
+        a.z = fmaf(v.a.z, w[i], a.z); a.w = fmaf(v.a.w, w[i], a.w);
+        b.x = fmaf(v.b.x, w[i], b.x); b.y = fmaf(v.b.y, w[i], b.y);
+        b.z = fmaf(v.b.z, w[i], b.z); b.w = fmaf(v.b.w, w[i], b.w);
+    }
+    if (!(ws > 0.0f)) return false;
+    const float iw = 1.0f / ws;
+    out.a = make_float4(a.x * iw, a.y * iw, a.z * iw, a.w * iw);
+    out.b = make_float4(b.x * iw, b.y * iw, b.z * iw, b.w * iw);
+    return true;
+}
+
 // Redoes the first m (<= 32, <= Q.n) queued pairs with the FP64 chain of the
 // PLAIN form, one per lane; credits each to its sample (serially, in queue
 // order, by the first lane of each run of one slot's entries), writes the TOD
-// of every sample left with nothing queued, and drops the m entries.
-template <class Action>
+// of every sample left with nothing queued, and drops the m entries.  kBil:
+// the beam value is PLAIN's bilinear one instead of the nearest pixel's.
+template <bool kBil = false, class Action>
 __device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& Q, int lane,
                                       unsigned int* err, Action& act)
 {
@@ -262,10 +370,15 @@ __device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& 
         const int pix = S.q[lane];
         double rho, sig, chi;
         const long long bp = pair_beam_pixel(hs, P.hb, pix, P.ra, P.dec, P.psi, &rho, &sig, &chi);
-        if (bp < 0)
+        if constexpr (kBil) {
+            F8 Bv;
+            if (bilinear_f64(P.hb, P.npix_beam, rho, sig, P.beam, Bv))
+                act.deferred(P, pix, Bv, (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+        } else if (bp < 0) {
             record(err, kCheckBeamIndex);
-        else if (bp < P.npix_beam)
+        } else if (bp < P.npix_beam) {
             act.deferred(P, pix, P.beam[bp], (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+        }
     }
     if (Action::kSums) {
         S.ta[lane] = ta;
@@ -310,11 +423,11 @@ __device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& 
 // Redoes every queued pair (at a sample boundary, where fewer than 32 are
 // queued): all slots are free afterwards.  Called once more before a warp
 // leaves the kernel.
-template <class Action>
+template <bool kBil = false, class Action>
 __device__ __forceinline__ void flush(const Hpx& hs, WarpSmem& S, Queue& Q, int lane,
                                       unsigned int* err, Action& act)
 {
-    if (Q.n > 0) drain(hs, Q.n, S, Q, lane, err, act);
+    if (Q.n > 0) drain<kBil>(hs, Q.n, S, Q, lane, err, act);
 }
 
 // sin(x) and 1 - cos(x): Taylor series for |x| <= 0.5 (truncation below
@@ -361,8 +474,9 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
 // pairs.  With kSums the TOD is written to `o` now, or by the drain that
 // redoes the sample's last queued pair.  nfall counts queued pairs and npairs
 // the disc pairs (lane 0 only); cmax (kCalib) is the worst FP32 decision
-// error over the non-queued pairs, in units of the margin.
-template <bool kCalib, class Action>
+// error over the non-queued pairs, in units of the margin.  kBil: bilinear
+// beam lookup (bilinear_f32; only the degenerate pairs are queued).
+template <bool kCalib, bool kBil = false, class Action>
 __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const Hpx& hb,
                                        const Beam& B, double ra,
                                        double dec, double pa, const Out& o, WarpSmem& S,
@@ -387,7 +501,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
     // redoing the whole queue
     const int slot = Qs.cur;
     Qs.cur = slot + 1 == kPend ? 0 : slot + 1;
-    if (S.p[slot].left > 0) flush(hs, S, Qs, lane, err, act);
+    if (S.p[slot].left > 0) flush<kBil>(hs, S, Qs, lane, err, act);
     if (lane == 0) {
         Pend& Ps = S.p[slot];
         Ps.hb = hb;
@@ -540,38 +654,53 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                     }
                     const float tp = quarter_turns(yy, xx);
                     const float r = B.rscale * (q * rsqrtf(q));
-                    const float av = tp * r;
-                    const float bv = (1.0f - tp) * r;
-                    const int jp = (int)av, jm = (int)bv;
-                    const int ir = jp + jm + 1;
-                    const float cv = tp * (float)ir;
-                    const int ipr = (int)cv;
-                    const float m = kMarginRel * (r + 1.0f);
-                    fb = q < kTinyQ || near_int(av, m) || near_int(bv, m) ||
-                         near_int(cv, kMarginRel * ((float)ir + 1.0f));
-                    if (kCalib && !fb) {
-                        double rho, sig, chi;
-                        (void)pair_beam_pixel(hs, hb, pix, F.ra, F.dec, F.psi, &rho, &sig, &chi);
-                        const double tt = fmodulo(sig * kInvHalfPi, 4.0);
-                        const double tpd = tt - floor(tt);
-                        const double rd = (double)B.nside * sqrt(3.0 * (1.0 - cos(rho)));
-                        const double e1 = fabs(av - tpd * rd) / (r + 1.0);
-                        const double e2 = fabs(bv - (1.0 - tpd) * rd) / (r + 1.0);
-                        const double e3 = fabs(cv - tpd * (double)ir) / ((double)ir + 1.0);
-                        cmax = fmaxf(cmax, (float)fmax(fmax(e1, e2), e3) / kMarginRel);
-                    }
-                    if (!fb) {
-                        const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
-                        if (bp >= 0 && bp < B.npix) {
-                            // exp(2i (beta + alpha)) = w^2 / |w|^2, w = (db + i nb)(v + i u),
-                            // then rotated by exp(2i psi)
-                            const float wr = fmaf(db, v_n, -nb * u_e);
-                            const float wi = fmaf(db, u_e, nb * v_n);
-                            const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
-                            const float er = fmaf(wr, wr, -wi * wi) * iw;
-                            const float ei = 2.0f * wr * wi * iw;
-                            act.pair(pix, act.fetch(pix), B.beam[bp], fmaf(er, F.c2p, -ei * F.s2p),
-                                     fmaf(ei, F.c2p, er * F.s2p));
+                    // exp(2i (beta + alpha)) = w^2 / |w|^2, w = (db + i nb)(v + i u),
+                    // then rotated by exp(2i psi)
+                    auto phasor = [&](float& c2, float& s2) {
+                        const float wr = fmaf(db, v_n, -nb * u_e);
+                        const float wi = fmaf(db, u_e, nb * v_n);
+                        const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
+                        const float er = fmaf(wr, wr, -wi * wi) * iw;
+                        const float ei = 2.0f * wr * wi * iw;
+                        c2 = fmaf(er, F.c2p, -ei * F.s2p);
+                        s2 = fmaf(ei, F.c2p, er * F.s2p);
+                    };
+                    if constexpr (kBil) {
+                        fb = q < kTinyQ;
+                        F8 Bv;
+                        if (!fb && bilinear_f32(B, qd, tp, r, Bv)) {
+                            float c2, s2;
+                            phasor(c2, s2);
+                            act.pair(pix, act.fetch(pix), Bv, c2, s2);
+                        }
+                    } else {
+                        const float av = tp * r;
+                        const float bv = (1.0f - tp) * r;
+                        const int jp = (int)av, jm = (int)bv;
+                        const int ir = jp + jm + 1;
+                        const float cv = tp * (float)ir;
+                        const int ipr = (int)cv;
+                        const float m = kMarginRel * (r + 1.0f);
+                        fb = q < kTinyQ || near_int(av, m) || near_int(bv, m) ||
+                             near_int(cv, kMarginRel * ((float)ir + 1.0f));
+                        if (kCalib && !fb) {
+                            double rho, sig, chi;
+                            (void)pair_beam_pixel(hs, hb, pix, F.ra, F.dec, F.psi, &rho, &sig, &chi);
+                            const double tt = fmodulo(sig * kInvHalfPi, 4.0);
+                            const double tpd = tt - floor(tt);
+                            const double rd = (double)B.nside * sqrt(3.0 * (1.0 - cos(rho)));
+                            const double e1 = fabs(av - tpd * rd) / (r + 1.0);
+                            const double e2 = fabs(bv - (1.0 - tpd) * rd) / (r + 1.0);
+                            const double e3 = fabs(cv - tpd * (double)ir) / ((double)ir + 1.0);
+                            cmax = fmaxf(cmax, (float)fmax(fmax(e1, e2), e3) / kMarginRel);
+                        }
+                        if (!fb) {
+                            const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
+                            if (bp >= 0 && bp < B.npix) {
+                                float c2, s2;
+                                phasor(c2, s2);
+                                act.pair(pix, act.fetch(pix), B.beam[bp], c2, s2);
+                            }
                         }
                     }
                 }
@@ -590,7 +719,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                     S.p[slot].left += __popc(mk);
                 }
                 __syncwarp();
-                if (Qs.n >= 32) drain(hs, 32, S, Qs, lane, err, act);
+                if (Qs.n >= 32) drain<kBil>(hs, 32, S, Qs, lane, err, act);
             }
         }
         __syncwarp();

@@ -176,6 +176,51 @@ def test_bilinear_matches_oracle(gpu, oracle_mod, golden_ellip):
     assert rel_max(pa_, fa) < 1e-6 and rel_max(pb_, fb) < 1e-6
 
 
+@pytest.mark.parametrize("case", ["golden_c1", "golden_ellip"])
+def test_tuned_bilinear_matches_plain(gpu, oracle_mod, case, request):
+    """TUNED with the bilinear lookup builds get_interpol's stencil in FP32
+    (continuous weights: no FP64 re-evaluation except at the boresight).
+    Against PLAIN's FP64 stencil and the FP64 oracle: the FP32 errors of r and
+    sigma (~1e-7 relative) move the weights by ~1e-5 at most, times the beam's
+    change over one pixel, so 1e-6 (rms) and 1e-5 (max) of the TOD rms."""
+    g = request.getfixturevalue(case)
+    n = g["ra"].size
+    c = make_conv(g, form="tuned", ptg64=True)
+    c.set_interp(True)
+    a, b = run(c, n, np.float64)
+    p = make_conv(g, form="plain", ptg64=True)
+    p.set_interp(True)
+    pa_, pb_ = run(p, n, np.float64)
+    oa, ob = oracle_mod.convolve_f64(g["ra"].astype(np.float64), g["dec"].astype(np.float64),
+                                     g["pa"].astype(np.float64), int(g["nside_sky"]),
+                                     g["sky"].astype(np.float32).astype(np.float64),
+                                     int(g["nside_beam"]), g["beam_a"].astype(np.float64),
+                                     g["beam_b"].astype(np.float64), interp=1)
+    rms = float(np.sqrt(np.mean(oa ** 2)))
+    for mine, ref in ((a, pa_), (b, pb_), (a, oa), (b, ob)):
+        d = mine - ref
+        assert np.sqrt(np.mean(d ** 2)) <= 1e-6 * rms
+        assert np.abs(d).max() <= 1e-5 * rms
+    # the nearest lookup is unchanged by switching back
+    c.set_interp(False)
+    na, _ = run(c, n, np.float64)
+    q = make_conv(g, form="tuned", ptg64=True)
+    qa, _ = run(q, n, np.float64)
+    assert np.array_equal(na, qa)
+
+
+def test_bilinear_adjoint_is_refused(gpu, golden_ellip):
+    """The adjoint transposes the nearest-pixel lookup only."""
+    from pisco4cmb_gb300 import PiscoError
+
+    g = golden_ellip
+    c = make_conv(g, form="tuned")
+    c.set_interp(True)
+    n = g["ra"].size
+    with pytest.raises(PiscoError):
+        c.adjoint(np.ones(n, np.float32), np.ones(n, np.float32))
+
+
 def test_polflag_tail_and_determinism(gpu, golden_c1):
     from pisco4cmb_gb300 import PiscoInvalidArgument, RunConfig
 
