@@ -249,9 +249,10 @@ __device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan&
 // Bilinear beam value of the PLAIN form (HEALPix get_interpol in FP64; the
 // weights of stencil pixels outside the stored map are dropped and the rest
 // renormalised; the value rounded to float).  false: no stencil pixel lies in
-// the map.
-__device__ __forceinline__ bool bilinear_f64(const Hpx& hb, int npb, double rho, double sig,
-                                             const F8* beam, F8& out)
+// the map.  Not inlined: only the degenerate boresight pairs take it, and
+// inlined its FP64 stencil would spill registers of the main pair loop.
+static __device__ __noinline__ bool bilinear_f64(const Hpx& hb, int npb, double rho,
+                                                 double sig, const F8* beam, F8& out)
 {
     int64_t px[4];
     double w[4];
@@ -297,8 +298,6 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
     const float c = 1.0f / (2.4494897427831781f * (float)B.nside);  // 1 / (sqrt(6) nside)
     const float c2 = c * c;
     const int k = (int)r;  // ring above (0 above the first ring)
-    int px[4];
-    float w[4];
     // longitude interpolation on ring i: pixels start + i1, start + i1 + 1
     auto ring = [&](int i, int& p1, int& p2, float& w1, float& w2) {
         const float t = fmaf(tp, (float)i, -0.5f);
@@ -314,37 +313,38 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
         w1 = 1.0f - f;
         w2 = f;
     };
-    if (k == 0) {
-        ring(1, px[2], px[3], w[2], w[3]);
-        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
-        const float f = 0.25f * (1.0f - wt);
-        w[0] = f;
-        w[1] = f;
-        w[2] = fmaf(w[2], wt, f);
-        w[3] = fmaf(w[3], wt, f);
-        px[0] = (px[2] + 2) & 3;
-        px[1] = (px[3] + 2) & 3;
-    } else {
-        ring(k, px[0], px[1], w[0], w[1]);
-        ring(k + 1, px[2], px[3], w[2], w[3]);
-        const float kf = (float)k;
-        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
-        w[0] *= 1.0f - wt;
-        w[1] *= 1.0f - wt;
-        w[2] *= wt;
-        w[3] *= wt;
-    }
+    // stencil pixels are added as soon as their weight is known, in
+    // get_interpol's order; pixels beyond the stored map are dropped
     float ws = 0.0f;
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        if (px[i] < 0 || px[i] >= B.npix) continue;
-        ws += w[i];
-        const F8 v = B.beam[px[i]];
-        a.x = fmaf(v.a.x, w[i], a.x); a.y = fmaf(v.a.y, w[i], a.y);
-        a.z = fmaf(v.a.z, w[i], a.z); a.w = fmaf(v.a.w, w[i], a.w);
-        b.x = fmaf(v.b.x, w[i], b.x); b.y = fmaf(v.b.y, w[i], b.y);
-        b.z = fmaf(v.b.z, w[i], b.z); b.w = fmaf(v.b.w, w[i], b.w);
+    auto add = [&](int p, float w) {
+        if (p >= B.npix) return;
+        ws += w;
+        const F8 v = B.beam[p];
+        a.x = fmaf(v.a.x, w, a.x); a.y = fmaf(v.a.y, w, a.y);
+        a.z = fmaf(v.a.z, w, a.z); a.w = fmaf(v.a.w, w, a.w);
+        b.x = fmaf(v.b.x, w, b.x); b.y = fmaf(v.b.y, w, b.y);
+        b.z = fmaf(v.b.z, w, b.z); b.w = fmaf(v.b.w, w, b.w);
+    };
+    int p1, p2;
+    float w1, w2;
+    if (k == 0) {
+        ring(1, p1, p2, w1, w2);
+        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
+        const float f = 0.25f * (1.0f - wt);
+        add((p1 + 2) & 3, f);
+        add((p2 + 2) & 3, f);
+        add(p1, fmaf(w1, wt, f));
+        add(p2, fmaf(w2, wt, f));
+    } else {
+        const float kf = (float)k;
+        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
+        ring(k, p1, p2, w1, w2);
+        add(p1, w1 * (1.0f - wt));
+        add(p2, w2 * (1.0f - wt));
+        ring(k + 1, p1, p2, w1, w2);
+        add(p1, w1 * wt);
+        add(p2, w2 * wt);
     }
     if (!(ws > 0.0f)) return false;
     const float iw = 1.0f / ws;
