@@ -934,7 +934,30 @@ def run_bilinear_study(args):
 
     reps = max(3, min(args.steps, 5))
     t_near, _ = timed(conv("tuned", False, n), n, reps)
-    t_bil, a_bil = timed(conv("tuned", True, n), n, reps)
+    cb = conv("tuned", True, n)
+    t_bil, a_bil = timed(cb, n, reps)
+
+    # adjoint of the bilinear lookup: deterministic sky (I, Q, U), atomic sky + beam
+    rng = np.random.default_rng(20261203)
+    g = [torch.tensor(rng.normal(size=n).astype(np.float32), device="cuda") for _ in range(2)]
+    gsky = torch.empty((12 * wl["nside_sky"] ** 2, 4), dtype=torch.float32, device="cuda")
+    gbeam = torch.empty((wl["beam"].nPixels, 8), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    def adj_time(det, beam):
+        cb.adjoint_device(g[0].data_ptr(), g[1].data_ptr(), False, gsky.data_ptr(),
+                          gbeam.data_ptr() if beam else 0, deterministic=det, stream=cs,
+                          sky_iqu=True)  # warm-up
+        e0.record()
+        cb.adjoint_device(g[0].data_ptr(), g[1].data_ptr(), False, gsky.data_ptr(),
+                          gbeam.data_ptr() if beam else 0, deterministic=det, stream=cs,
+                          sky_iqu=True)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    t_adj_det = adj_time(True, False)
+    t_adj_atom = adj_time(False, True)
     m = min(n, args.plain_samples)
     t_plain, _ = timed(conv("plain", True, m), m, 1)
     k = min(n, args.fp64_samples)
@@ -945,6 +968,10 @@ def run_bilinear_study(args):
             "tuned_nearest": {"ms": t_near * 1e3, "samples_per_s": n / t_near},
             "tuned_bilinear": {"ms": t_bil * 1e3, "samples_per_s": n / t_bil,
                                "over_nearest": t_bil / t_near},
+            "adjoint_bilinear": {"deterministic_sky_iqu_ms": t_adj_det * 1e3,
+                                 "deterministic_sky_iqu_over_forward": t_adj_det / t_bil,
+                                 "atomic_sky_iqu_and_beam_ms": t_adj_atom * 1e3,
+                                 "atomic_sky_iqu_and_beam_over_forward": t_adj_atom / t_bil},
             "plain_bilinear": {"samples_per_s": m / t_plain, "sample": m,
                                "tuned_over_plain": (n / t_bil) / (m / t_plain)},
             "tuned_bilinear_vs_fp64_bilinear": {"rms": float(np.sqrt(np.mean(d ** 2))) / rms,

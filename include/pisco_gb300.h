@@ -53,8 +53,8 @@ typedef enum pisco_form {
 
 /* Beam lookup: nearest beam pixel (the reference's live path,
  * convolver.cpp:186-203) or 4-pixel bilinear (the commented-out
- * get_interpol block, convolver.cpp:162-185).  Every forward form takes
- * both; the adjoint and the batched launch take the nearest lookup only
+ * get_interpol block, convolver.cpp:162-185).  Every forward form and the
+ * adjoint take both; the batched launch takes the nearest lookup only
  * (PISCO_ERR_UNSUPPORTED otherwise). */
 typedef enum pisco_interp { PISCO_BEAM_NEAREST = 0, PISCO_BEAM_BILINEAR = 1 } pisco_interp;
 

@@ -9,7 +9,9 @@
 //   dL/da0(b) += ga I, dL/da1(b) += ga (Q c2 + U s2), dL/da2(b) += ga (U c2 - Q s2), ...
 // for every pair (s, p) with beam pixel b, with the pair set and the beam
 // pixel of each pair taken by exactly the TUNED forward's geometry
-// (tuned_core.cuh), so the adjoint is the transpose of that operator.
+// (tuned_core.cuh), so the adjoint is the transpose of that operator.  With
+// the bilinear lookup the pair's beam value is sum_i w_i beam[b_i], and its
+// beam gradient goes to the stencil pixels b_i by the weights w_i.
 //
 // Accumulation, two variants:
 //  * ATOMIC: float atomics (vector float4 adds for the sky) -- fast, but the
@@ -33,6 +35,7 @@ constexpr int kAW = PISCO_TUNED_WARPS;
 template <bool kFixed>
 struct Scatter {
     static constexpr bool kSums = false;
+    static constexpr bool kStencil = false;  // the sky gradient needs the interpolated value only
     float ga, gb;
     float* gsky;                  // ATOMIC: float4-interleaved [npix][4]
     unsigned long long* gsky_fx;  // DETERMINISTIC: int64 [npix][4]
@@ -82,11 +85,14 @@ struct Scatter {
     }
 };
 
-// Sky and beam gradient: the beam pixel index is recovered as &B - base
-// (the action receives a reference to beam[bp] itself).
+// Sky and beam gradient: with the nearest lookup the beam pixel index is
+// recovered as &B - base (the action receives a reference to beam[bp]
+// itself); with the bilinear one the action gets the stencil and spreads
+// each pair's beam gradient over its (up to) four pixels by their weights.
 template <bool kFixed>
 struct ScatterBeam {
     static constexpr bool kSums = false;
+    static constexpr bool kStencil = true;
     float ga, gb;
     const F8* beam_base;
     const float4* sky;
@@ -115,6 +121,38 @@ struct ScatterBeam {
         scatter(ga, gb, pix, S, B, c2, s2);
     }
 
+    __device__ __forceinline__ void pair_stencil(int pix, const float4& S, const int px[4],
+                                                 const float w[4], float c2, float s2) const
+    {
+        scatter_stencil(ga, gb, pix, S, px, w, c2, s2);
+    }
+    __device__ __forceinline__ void deferred_stencil(const tuned::Pend& p, int pix, const int px[4],
+                                                     const float w[4], float c2, float s2) const
+    {
+        scatter_stencil(p.ga, p.gb, pix, fetch(pix), px, w, c2, s2);
+    }
+
+    // d(tod)/d(beam) of one pair, times the TOD weights: 8 values (a.IQUV, b.IQUV)
+    __device__ __forceinline__ static void beam_grad(float wa, float wb, const float4& S, float c2,
+                                                     float s2, float v[8])
+    {
+        const float qa = S.y * c2 + S.z * s2, ua = S.z * c2 - S.y * s2;
+        v[0] = wa * S.x; v[1] = wa * qa; v[2] = wa * ua; v[3] = wa * S.w;
+        v[4] = wb * S.x; v[5] = -wb * qa; v[6] = -wb * ua; v[7] = wb * S.w;
+    }
+    __device__ __forceinline__ void add_beam(long long bp, const float v[8], float w) const
+    {
+        if (kFixed) {
+            unsigned long long* p = gbeam_fx + 8 * bp;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) atomicAdd(p + k, Scatter<kFixed>::fx(v[k] * w, sbeam));
+        } else {
+            float4* p = reinterpret_cast<float4*>(gbeam) + 2 * bp;
+            atomicAdd(p, make_float4(v[0] * w, v[1] * w, v[2] * w, v[3] * w));
+            atomicAdd(p + 1, make_float4(v[4] * w, v[5] * w, v[6] * w, v[7] * w));
+        }
+    }
+
     __device__ __forceinline__ void scatter(float wa, float wb, int pix, const float4& S,
                                            const F8& B, float c2, float s2) const
     {
@@ -123,9 +161,9 @@ struct ScatterBeam {
                                      nullptr, nullptr, ssky, sbeam, want_v};
             sc.scatter(wa, wb, pix, B, c2, s2);
         }
+        float v[8];
+        beam_grad(wa, wb, S, c2, s2, v);
         const long long bp = &B - beam_base;
-        const float qa = S.y * c2 + S.z * s2, ua = S.z * c2 - S.y * s2;
-        const float v[8] = {wa * S.x, wa * qa, wa * ua, wa * S.w, wb * S.x, -wb * qa, -wb * ua, wb * S.w};
         if (kFixed) {
             unsigned long long* p = gbeam_fx + 8 * bp;
 #pragma unroll
@@ -136,9 +174,41 @@ struct ScatterBeam {
             atomicAdd(p + 1, make_float4(v[4], v[5], v[6], v[7]));
         }
     }
+
+    // bilinear lookup: the pair's beam value is sum_i w_i beam[px_i] (w
+    // renormalised over the stored map), so each stencil pixel gets w_i of
+    // the pair's beam gradient; the sky gradient uses the interpolated value
+    __device__ __forceinline__ void scatter_stencil(float wa, float wb, int pix, const float4& S,
+                                                   const int px[4], const float w[4], float c2,
+                                                   float s2) const
+    {
+        if (want_sky) {
+            F8 B;
+            B.a = make_float4(0.f, 0.f, 0.f, 0.f);
+            B.b = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (w[i] == 0.0f) continue;
+                const F8 v = beam_base[px[i]];
+                B.a.x = fmaf(v.a.x, w[i], B.a.x); B.a.y = fmaf(v.a.y, w[i], B.a.y);
+                B.a.z = fmaf(v.a.z, w[i], B.a.z); B.a.w = fmaf(v.a.w, w[i], B.a.w);
+                B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);
+                B.b.z = fmaf(v.b.z, w[i], B.b.z); B.b.w = fmaf(v.b.w, w[i], B.b.w);
+            }
+            const Scatter<kFixed> sc{wa,      wb,   gsky,  gsky_fx, nullptr,
+                                     nullptr, nullptr, ssky, sbeam, want_v};
+            sc.scatter(wa, wb, pix, B, c2, s2);
+        }
+        float v[8];
+        beam_grad(wa, wb, S, c2, s2, v);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (w[i] != 0.0f) add_beam(px[i], v, w[i]);
+    }
 };
 
-template <class Act>
+// kBil: the transpose of the TUNED forward with the bilinear beam lookup.
+template <class Act, bool kBil>
 __global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(AdjArgs a, Act proto)
 {
     __shared__ tuned::WarpSmem sm[kAW];
@@ -162,10 +232,10 @@ __global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(Adj
         if (ga == 0.0 && gb == 0.0) continue;
         act.ga = (float)ga;
         act.gb = (float)gb;
-        tuned::sample<false>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], none, S, Q, lane,
-                             a.err, act, nfall, cmax, npairs);
+        tuned::sample<false, kBil>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], none, S, Q,
+                                   lane, a.err, act, nfall, cmax, npairs);
     }
-    tuned::flush(hs, S, Q, lane, a.err, act);
+    tuned::flush<kBil>(hs, S, Q, lane, a.err, act);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
 }
 
@@ -238,8 +308,13 @@ template <class Act>
 cudaError_t launch_act(const AdjArgs& a, const Act& act, int sm_count, cudaStream_t st)
 {
     const long long need = (a.n + kAW - 1) / kAW;
-    long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act>, kAW * 32);
-    adjoint_kernel<Act><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+    if (a.interp == 1) {
+        long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, true>, kAW * 32);
+        adjoint_kernel<Act, true><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+    } else {
+        long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, false>, kAW * 32);
+        adjoint_kernel<Act, false><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+    }
     return cudaGetLastError();
 }
 

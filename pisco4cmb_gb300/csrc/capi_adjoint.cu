@@ -111,9 +111,6 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
 {
     if (!c) return PISCO_ERR_INVALID_ARGUMENT;
     if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
-    if (c->interp != PISCO_BEAM_NEAREST)
-        return fail(c, PISCO_ERR_UNSUPPORTED, "the adjoint is the transpose of the nearest-pixel "
-                                              "beam lookup; set PISCO_BEAM_NEAREST");
     if (begin < 0 || n < 0 || begin + n > c->nsamples)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sample range outside the scan");
     if (n > 0 && (!d_ga || !d_gb)) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "TOD gradients are NULL");
@@ -150,6 +147,7 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     a.g_b = d_gb;
     a.g_f64 = g_dtype == PISCO_FLOAT64;
     a.want_v = sky_iqu ? 0 : 1;
+    a.interp = (int)c->interp;
     st = c->range_order(begin, n, s, &a.order);
     if (st != PISCO_OK) return st;
     a.err = c->d_err;
@@ -204,10 +202,14 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
             CK(cudaMemcpyAsync(&h[2], c->red + 512, sizeof(double), cudaMemcpyDeviceToHost, s), "bound D2H");
             CK(cudaStreamSynchronize(s), "bound sync");
         }
-        // |contribution to a sky total| <= 2 max|beam| (|ga| + |gb|), one per sample;
+        // |contribution to a sky total| <= 2 max|beam| (|ga| + |gb|), one per sample
+        // (an interpolated beam value is a convex combination of beam values);
         // |contribution to a beam total| <= 2 max|sky| (|ga| + |gb|), at most K per sample
+        // (with the bilinear lookup a beam pixel is in the stencil of the pairs
+        // within one ring and one pixel of it: at most 4 K, weights <= 1)
         const double ratio = (double)c->nside_sky / (double)c->nside_beam;
-        const double K2 = std::ceil(2.0 * ratio * ratio) + 4.0;  // sky pixels per beam pixel
+        double K2 = std::ceil(2.0 * ratio * ratio) + 4.0;  // sky pixels per beam pixel
+        if (c->interp != PISCO_BEAM_NEAREST) K2 = 4.0 * K2 + 8.0;
         a.sky_scale = fixed_scale(2.0001 * h[1] * h[0]);
         a.beam_scale = fixed_scale(2.0001 * h[2] * h[0] * K2);
         if (d_gsky) {
@@ -250,9 +252,6 @@ pisco_status pisco_adjoint(pisco_ctx* c, const void* g_a, const void* g_b, pisco
                            pisco_adjoint_mode mode)
 {
     if (!c) return PISCO_ERR_INVALID_ARGUMENT;
-    if (c->interp != PISCO_BEAM_NEAREST)
-        return fail(c, PISCO_ERR_UNSUPPORTED, "the adjoint is the transpose of the nearest-pixel "
-                                              "beam lookup; set PISCO_BEAM_NEAREST");
     if (g_dtype != PISCO_FLOAT32 && g_dtype != PISCO_FLOAT64) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
     if (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
     if (!c->nside_sky) return fail(c, PISCO_ERR_NOT_READY, "no sky set");

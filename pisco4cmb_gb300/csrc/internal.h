@@ -139,6 +139,7 @@ struct AdjArgs {
     unsigned long long* gbeam_fx;  // fixed: [npixB][8] or null
     double sky_scale, beam_scale;  // fixed-point scales 2^S
     int want_v;                    // accumulate the sky gradient's V column
+    int interp;                    // 0 nearest, 1 bilinear beam lookup
     unsigned int* err;
     unsigned long long* fallbacks;
 };

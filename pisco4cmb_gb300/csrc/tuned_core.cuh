@@ -46,7 +46,12 @@
 //   void stash(Pend&)         per-sample data a queued pair needs later
 //   void deferred(const Pend&, int pix, const F8& beam, float c2, float s2,
 //                 float& ta, float& tb)      a re-evaluated pair
-// (c2, s2 = cos 2chi, sin 2chi; `beam` refers to the beam array element).
+//   kStencil                  true: with the bilinear lookup the action gets
+//                             the stencil instead of the interpolated value:
+//   void pair_stencil(int pix, P fetched, const int px[4], const float w[4], c2, s2)
+//   void deferred_stencil(const Pend&, int pix, const int px[4], const float w[4], c2, s2)
+// (c2, s2 = cos 2chi, sin 2chi; `beam` refers to the beam array element with
+// the nearest lookup, to the interpolated value with the bilinear one).
 #pragma once
 
 #include <math_constants.h>
@@ -274,6 +279,29 @@ static __device__ __noinline__ bool bilinear_f64(const Hpx& hb, int npb, double 
     return true;
 }
 
+// get_interpol's stencil in FP64 with the weights renormalised over the
+// pixels inside the stored map (pixels outside get weight 0), rounded to
+// float: what a beam-gradient scatter needs.  false: no pixel in the map.
+static __device__ __noinline__ bool stencil_f64(const Hpx& hb, int npb, double rho, double sig,
+                                                int px[4], float w[4])
+{
+    int64_t p[4];
+    double wd[4];
+    get_interpol(hb, rho, sig, p, wd);
+    double ws = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (p[i] >= 0 && p[i] < npb) ws += wd[i];
+    if (!(ws > 0.0)) return false;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool in = p[i] >= 0 && p[i] < npb;
+        px[i] = in ? (int)p[i] : 0;
+        w[i] = in ? (float)(wd[i] / ws) : 0.0f;
+    }
+    return true;
+}
+
 // (f(a) - f(b)) / (2c (a - b)) for f(x) = 2 asin(c x), the colatitude of ring
 // height x (x = nside sqrt(3 (1 - cos theta)), c = 1 / (sqrt(6) nside)), by
 // the asin series to c^4 (relative truncation below 1e-8 for theta <= 0.5).
@@ -353,6 +381,65 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
     return true;
 }
 
+// The stencil of bilinear_f32 itself: pixels and weights renormalised over
+// the pixels inside the stored map (outside: weight 0), for actions that
+// scatter into the beam (Action::kStencil).
+__device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, float r, int px[4],
+                                            float w[4])
+{
+    const float c = 1.0f / (2.4494897427831781f * (float)B.nside);
+    const float c2 = c * c;
+    const int k = (int)r;
+    auto ring = [&](int i, int& p1, int& p2, float& w1, float& w2) {
+        const float t = fmaf(tp, (float)i, -0.5f);
+        const float fl = floorf(t);
+        const float f = t - fl;
+        int i1 = (int)fl + qd * i, i2 = i1 + 1;
+        const int np = 4 * i;
+        if (i1 < 0) i1 += np;
+        if (i2 >= np) i2 -= np;
+        const int start = 2 * i * (i - 1);
+        p1 = start + i1;
+        p2 = start + i2;
+        w1 = 1.0f - f;
+        w2 = f;
+    };
+    if (k == 0) {
+        ring(1, px[2], px[3], w[2], w[3]);
+        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
+        const float f = 0.25f * (1.0f - wt);
+        w[0] = f;
+        w[1] = f;
+        w[2] = fmaf(w[2], wt, f);
+        w[3] = fmaf(w[3], wt, f);
+        px[0] = (px[2] + 2) & 3;
+        px[1] = (px[3] + 2) & 3;
+    } else {
+        ring(k, px[0], px[1], w[0], w[1]);
+        ring(k + 1, px[2], px[3], w[2], w[3]);
+        const float kf = (float)k;
+        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
+        w[0] *= 1.0f - wt;
+        w[1] *= 1.0f - wt;
+        w[2] *= wt;
+        w[3] *= wt;
+    }
+    float ws = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (px[i] >= B.npix) {
+            px[i] = 0;
+            w[i] = 0.0f;
+        }
+        ws += w[i];
+    }
+    if (!(ws > 0.0f)) return false;
+    const float iw = 1.0f / ws;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] *= iw;
+    return true;
+}
+
 // Redoes the first m (<= 32, <= Q.n) queued pairs with the FP64 chain of the
 // PLAIN form, one per lane; credits each to its sample (serially, in queue
 // order, by the first lane of each run of one slot's entries), writes the TOD
@@ -370,7 +457,12 @@ __device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& 
         const int pix = S.q[lane];
         double rho, sig, chi;
         const long long bp = pair_beam_pixel(hs, P.hb, pix, P.ra, P.dec, P.psi, &rho, &sig, &chi);
-        if constexpr (kBil) {
+        if constexpr (kBil && Action::kStencil) {
+            int px[4];
+            float w[4];
+            if (stencil_f64(P.hb, P.npix_beam, rho, sig, px, w))
+                act.deferred_stencil(P, pix, px, w, (float)cos(2.0 * chi), (float)sin(2.0 * chi));
+        } else if constexpr (kBil) {
             F8 Bv;
             if (bilinear_f64(P.hb, P.npix_beam, rho, sig, P.beam, Bv))
                 act.deferred(P, pix, Bv, (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
@@ -665,7 +757,16 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                         c2 = fmaf(er, F.c2p, -ei * F.s2p);
                         s2 = fmaf(ei, F.c2p, er * F.s2p);
                     };
-                    if constexpr (kBil) {
+                    if constexpr (kBil && Action::kStencil) {
+                        fb = q < kTinyQ;
+                        int px[4];
+                        float w[4];
+                        if (!fb && stencil_f32(B, qd, tp, r, px, w)) {
+                            float c2, s2;
+                            phasor(c2, s2);
+                            act.pair_stencil(pix, act.fetch(pix), px, w, c2, s2);
+                        }
+                    } else if constexpr (kBil) {
                         fb = q < kTinyQ;
                         F8 Bv;
                         if (!fb && bilinear_f32(B, qd, tp, r, Bv)) {
@@ -743,6 +844,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
 // Forward action: gather the sky, multiply by the beam, compensated sums.
 struct Gather {
     static constexpr bool kSums = true;
+    static constexpr bool kStencil = false;
     const float4* sky;
     float sa, ca, sb, cb;
     __device__ __forceinline__ void reset() { sa = ca = sb = cb = 0.0f; }

@@ -214,3 +214,31 @@ def test_autograd_against_finite_differences(gpu):
         fd = (loss64(sky0, pp) - loss64(sky0, pm)) / (2 * hk)
         ag = float(pt[k].grad)
         assert abs(fd - ag) <= 2e-3 * abs(fd) + 1e-9, (k, fd, ag)
+
+
+@pytest.mark.parametrize("deterministic", [True, False])
+def test_bilinear_adjoint_is_transpose(gpu, deterministic):
+    """With the bilinear lookup the TOD is linear in the sky and in the beam
+    maps (each pair's beam value is sum_i w_i beam[b_i]): <A x, y> ==
+    <x, A^T y> for both, with the TUNED forward's FP32 stencil on both sides."""
+    import torch
+
+    conv, sky, beam, ra, *_ = _case(seed=9)
+    npb = beam.nPixels
+    conv._keep_npb = npb
+    conv.set_interp(True)
+    n = ra.size
+    rng = np.random.default_rng(12)
+    ya, yb = rng.normal(size=n), rng.normal(size=n)
+    gs, gbm = _adj(conv, ya, yb, deterministic, beam=True)
+    ta, tb = _fwd(conv, n)
+    lhs = ta @ ya + tb @ yb
+    x4 = np.concatenate([sky, np.zeros((1, sky.shape[1]))]).astype(np.float32).astype(np.float64)
+    assert abs(lhs - float(np.sum(x4.T * gs))) <= 1e-6 * abs(lhs)
+    delta = rng.normal(size=(npb, 8)).astype(np.float32)
+    d = torch.tensor(delta, device="cuda")
+    torch.cuda.synchronize()
+    conv.set_beam_device(beam.nside, npb, d.data_ptr())
+    ta, tb = _fwd(conv, n)
+    lhs = ta @ ya + tb @ yb
+    assert abs(lhs - float(np.sum(delta.astype(np.float64) * gbm))) <= 1e-5 * abs(lhs)

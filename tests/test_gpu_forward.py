@@ -209,18 +209,6 @@ def test_tuned_bilinear_matches_plain(gpu, oracle_mod, case, request):
     assert np.array_equal(na, qa)
 
 
-def test_bilinear_adjoint_is_refused(gpu, golden_ellip):
-    """The adjoint transposes the nearest-pixel lookup only."""
-    from pisco4cmb_gb300 import PiscoError
-
-    g = golden_ellip
-    c = make_conv(g, form="tuned")
-    c.set_interp(True)
-    n = g["ra"].size
-    with pytest.raises(PiscoError):
-        c.adjoint(np.ones(n, np.float32), np.ones(n, np.float32))
-
-
 def test_polflag_tail_and_determinism(gpu, golden_c1):
     from pisco4cmb_gb300 import PiscoInvalidArgument, RunConfig
 
