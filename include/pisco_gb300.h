@@ -53,9 +53,8 @@ typedef enum pisco_form {
 
 /* Beam lookup: nearest beam pixel (the reference's live path,
  * convolver.cpp:186-203) or 4-pixel bilinear (the commented-out
- * get_interpol block, convolver.cpp:162-185).  Every forward form and the
- * adjoint take both; the batched launch takes the nearest lookup only
- * (PISCO_ERR_UNSUPPORTED otherwise). */
+ * get_interpol block, convolver.cpp:162-185).  The forward forms, the
+ * batched launch and the adjoint all take both. */
 typedef enum pisco_interp { PISCO_BEAM_NEAREST = 0, PISCO_BEAM_BILINEAR = 1 } pisco_interp;
 
 /* Order in which a launch processes the samples of its range (no reference

@@ -55,9 +55,6 @@ pisco_status validate(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "need 1..65536 detector descriptors");
     if (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad output dtype");
-    if (c->interp != PISCO_BEAM_NEAREST)
-        return fail(c, PISCO_ERR_UNSUPPORTED, "the batched launch uses the nearest-pixel beam "
-                                              "lookup; set PISCO_BEAM_NEAREST");
     if (!c->sky32 || !c->nside_sky) return fail(c, PISCO_ERR_NOT_READY, "no sky set");
     for (int d = 0; d < ndet; ++d) {
         const pisco_det_desc& x = dets[d];
@@ -82,8 +79,8 @@ std::string launch_key(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco
 {
     std::string k((const char*)dets, sizeof(pisco_det_desc) * (size_t)ndet);
     char tail[128];
-    std::snprintf(tail, sizeof tail, "|%d|%d|%p|%d", chunk, (int)out_dtype, (void*)c->sky32,
-                  c->nside_sky);
+    std::snprintf(tail, sizeof tail, "|%d|%d|%p|%d|%d", chunk, (int)out_dtype, (void*)c->sky32,
+                  c->nside_sky, (int)c->interp);
     return k + tail;
 }
 
@@ -234,6 +231,7 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         a.out_f64 = out_dtype == PISCO_FLOAT64;
         a.err = c->d_err;
         a.fallbacks = c->d_fallbacks;
+        a.interp = (int)c->interp;
         // capture (queue reset + kernel) once; replays reuse it
         if (c->graph_exec) {
             cudaGraphExecDestroy(c->graph_exec);

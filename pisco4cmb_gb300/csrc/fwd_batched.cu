@@ -54,6 +54,8 @@ struct ItemState {
     int state;  // 0: queue empty, 1: run, 2: bad item (skipped)
 };
 
+// kBil: bilinear beam lookup (tuned_core.cuh bilinear_f32).
+template <bool kBil>
 __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(BatchArgs a)
 {
     __shared__ tuned::WarpSmem sm[kBW];
@@ -102,11 +104,11 @@ __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(Bat
         for (long long p = T.begin + warp; p < T.end; p += kBW) {
             const long long s = T.order ? (long long)T.order[p] : p;  // sample of position p
             const tuned::Out o{T.out_a, T.out_b, s, a.out_f64};
-            tuned::sample<false>(hs, a.rings, T.hb, T.B, T.ra[s], T.dec[s], T.pa[s], o, S, Q, lane,
-                                 a.err, g, nfall, cmax, npairs);
+            tuned::sample<false, kBil>(hs, a.rings, T.hb, T.B, T.ra[s], T.dec[s], T.pa[s], o, S,
+                                       Q, lane, a.err, g, nfall, cmax, npairs);
         }
     }
-    tuned::flush(hs, S, Q, lane, a.err, g);
+    tuned::flush<kBil>(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
 }
 
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(Bat
 int batched_grid(int sm_count)
 {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel, kBW * 32, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false>, kBW * 32, 0) !=
             cudaSuccess ||
         nb < 1)
         nb = 1;
@@ -125,7 +127,8 @@ int batched_grid(int sm_count)
 cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st)
 {
     if (a.nitems <= 0) return cudaSuccess;
-    batched_kernel<<<grid, kBW * 32, 0, st>>>(a);
+    if (a.interp == 1) batched_kernel<true><<<grid, kBW * 32, 0, st>>>(a);
+    else batched_kernel<false><<<grid, kBW * 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -114,6 +114,7 @@ struct BatchArgs {
     int out_f64;
     unsigned int* err;
     unsigned long long* fallbacks;
+    int interp = 0;  // 0 nearest, 1 bilinear beam lookup
 };
 
 struct AdjArgs {
