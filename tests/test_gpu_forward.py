@@ -340,3 +340,64 @@ def test_largest_sky_and_beam(gpu, oracle_mod):
     assert pairs == ref_pairs
     for k in range(2):
         assert rel_max(outs["tuned"][k], outs["fp64"][k]) < 1e-6
+
+
+def test_random_configuration_sweep(gpu, oracle_mod):
+    """Seeded sweep of sky nside, beam nside, radius, ellipticity and
+    pointings (a tenth within the beam radius of either pole): TUNED against
+    the FP64 form with each lookup (nearest: rms error 1e-6 of the TOD rms and
+    max error 1e-6 of the largest TOD value, every decision within its margin
+    and the disc exactly HEALPix's; bilinear: 1e-5), PLAIN against FP64 (1e-6).
+    Discs hold a few sky pixels at least (radius >= 1.5 sky pixels): with
+    mostly empty discs the TOD is mostly zero and an error relative to its
+    rms says little."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky, synth
+
+    rng = np.random.default_rng(20261203)
+    for _ in range(24):
+        nss = int(2 ** rng.integers(4, 11))            # 16 .. 1024
+        nsb = int(2 ** rng.integers(7, 12))            # 128 .. 2048
+        pix_deg = np.rad2deg(np.sqrt(4 * np.pi / (12 * nss * nss)))
+        rdeg = float(rng.uniform(max(0.3, 1.5 * pix_deg), max(6.0, 3.0 * pix_deg)))
+        while not (nsb * np.sqrt(3 * (1 - np.cos(np.deg2rad(rdeg)))) + 2 < nsb):
+            nsb *= 2
+        npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(rdeg))
+        beam = PolBeam(nsb, npb, float(rng.uniform(0, 0.05)), "p")
+        fx, fy = synth.elliptical_fwhm(rdeg / 2.5, float(rng.uniform(-0.1, 0.1)))
+        beam.make_unpol_gaussian_elliptical_beams(fx, fy, float(rng.uniform(0, 180)))
+        beam.build(nss)
+        n = 1500
+        ra = rng.uniform(0, 2 * np.pi, n)
+        dec = np.arcsin(rng.uniform(-1, 1, n))
+        k = n // 20
+        dec[:k] = np.pi / 2 - rng.uniform(0, np.deg2rad(rdeg), k)
+        dec[k:2 * k] = -np.pi / 2 + rng.uniform(0, np.deg2rad(rdeg), k)
+        pa = rng.uniform(-np.pi, np.pi, n)
+        sky = rng.normal(size=(3, 12 * nss * nss)).astype(np.float32)
+        out = {}
+        for form, interp in (("fp64", False), ("tuned", False), ("plain", False),
+                             ("fp64", True), ("tuned", True)):
+            c = GPUConvolver(form=form)
+            c.update_sky(Sky(nss, *sky, None))
+            c.update_beam(beam)
+            c.set_interp(interp)
+            c.update_scan(Scan(n, ra, dec, pa))
+            a = np.zeros(n)
+            b = np.zeros(n)
+            c.exec_convolution(a, b)
+            out[form, interp] = (a, b)
+            if form == "tuned" and not interp:
+                worst, tp = c.tuned_calibrate(with_pairs=True)
+                assert tp == c.count_pairs() and worst < 0.5, (nss, nsb, rdeg, worst)
+            c.close()
+        case = (nss, nsb, round(rdeg, 3))
+
+        def close(x, ref, tol):
+            d = x - ref
+            return (np.sqrt(np.mean(d ** 2)) <= tol * np.sqrt(np.mean(ref ** 2))
+                    and np.abs(d).max() <= tol * np.abs(ref).max())
+
+        for x in range(2):
+            assert close(out["tuned", False][x], out["fp64", False][x], 1e-6), case
+            assert close(out["plain", False][x], out["fp64", False][x], 1e-6), case
+            assert close(out["tuned", True][x], out["fp64", True][x], 1e-5), case
