@@ -242,3 +242,57 @@ def test_bilinear_adjoint_is_transpose(gpu, deterministic):
     ta, tb = _fwd(conv, n)
     lhs = ta @ ya + tb @ yb
     assert abs(lhs - float(np.sum(delta.astype(np.float64) * gbm))) <= 1e-5 * abs(lhs)
+
+
+def test_adjoint_transpose_sweep(gpu):
+    """Seeded sweep of sky/beam resolutions, radii and pole-heavy pointings:
+    <A x, y> == <x, A^T y> for the sky (I, Q, U, V) and for the beam maps,
+    with each lookup and each accumulation mode."""
+    import torch
+
+    import oracle as O
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Sky, synth
+
+    rng = np.random.default_rng(31)
+    for _ in range(6):
+        nss = int(2 ** rng.integers(4, 9))   # 16 .. 256
+        nsb = int(2 ** rng.integers(7, 11))  # 128 .. 1024
+        pix_deg = np.rad2deg(np.sqrt(4 * np.pi / (12 * nss * nss)))
+        rdeg = float(rng.uniform(max(0.5, 1.5 * pix_deg), max(5.0, 3.0 * pix_deg)))
+        npb = O.beam_npix_for_radius(nsb, np.deg2rad(rdeg))
+        beam = PolBeam(nsb, npb, 0.01, "p")
+        fx, fy = synth.elliptical_fwhm(rdeg / 2.5, float(rng.uniform(-0.1, 0.1)))
+        beam.make_unpol_gaussian_elliptical_beams(fx, fy, float(rng.uniform(0, 180)))
+        beam.build(nss)
+        n = 1200
+        ra = rng.uniform(0, 2 * np.pi, n)
+        dec = np.arcsin(rng.uniform(-1, 1, n))
+        dec[:60] = np.pi / 2 - rng.uniform(0, np.deg2rad(rdeg), 60)
+        pa = rng.uniform(0, np.pi, n)
+        sky = rng.normal(size=(4, 12 * nss * nss)).astype(np.float32)
+        delta = rng.normal(size=(npb, 8)).astype(np.float32)
+        ya, yb = rng.normal(size=n), rng.normal(size=n)
+        for interp in (False, True):
+            conv = GPUConvolver(form="tuned")
+            conv.update_sky(Sky(nss, *sky))
+            conv.update_beam(beam)
+            conv.set_interp(interp)
+            t = [torch.tensor(x, device="cuda") for x in (ra, dec, pa)]
+            torch.cuda.synchronize()
+            conv.set_scan_device(n, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr())
+            conv._keep_npb = npb
+            ta, tb = _fwd(conv, n)
+            lhs_sky = ta @ ya + tb @ yb
+            for det in (True, False):
+                gs, gbm = _adj(conv, ya, yb, det, beam=True)
+                assert abs(lhs_sky - float(np.sum(sky.astype(np.float64).T * gs))) <= \
+                    1e-5 * abs(lhs_sky), (nss, nsb, rdeg, interp, det)
+                d = torch.tensor(delta, device="cuda")
+                torch.cuda.synchronize()
+                conv.set_beam_device(nsb, npb, d.data_ptr())
+                xa, xb = _fwd(conv, n)
+                lhs_beam = xa @ ya + xb @ yb
+                assert abs(lhs_beam - float(np.sum(delta.astype(np.float64) * gbm))) <= \
+                    1e-5 * abs(lhs_beam), (nss, nsb, rdeg, interp, det)
+                conv.update_beam(beam)
+            conv.close()
