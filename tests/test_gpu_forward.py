@@ -401,3 +401,44 @@ def test_random_configuration_sweep(gpu, oracle_mod):
             assert close(out["tuned", False][x], out["fp64", False][x], 1e-6), case
             assert close(out["plain", False][x], out["fp64", False][x], 1e-6), case
             assert close(out["tuned", True][x], out["fp64", True][x], 1e-5), case
+
+
+def test_wide_fine_beam_both_lookups(gpu, oracle_mod):
+    """Beam nside 8192 out to 5 deg (1,533,000 pixels; polar-cap rings up to
+    ~1,240, where the FP32 stencil's longitude weights carry ~1e-4 absolute
+    error): TUNED against the FP64 form with each lookup, nearest at the TUNED
+    tolerance (1e-6), bilinear at 1e-5 (rms and max, relative to the TOD)."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky
+
+    nss, nsb, rdeg = 256, 8192, 5.0
+    npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(rdeg))
+    beam = PolBeam(nsb, npb, 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(2.2, 1.8, 35.0)
+    beam.build(nss)
+    rng = np.random.default_rng(41)
+    n = 1000
+    ra = rng.uniform(0, 2 * np.pi, n)
+    dec = np.arcsin(rng.uniform(-1, 1, n))
+    dec[:50] = np.pi / 2 - rng.uniform(0, np.deg2rad(rdeg), 50)
+    pa = rng.uniform(0, np.pi, n)
+    sky = rng.normal(size=(3, 12 * nss * nss)).astype(np.float32)
+    out = {}
+    for form in ("tuned", "fp64"):
+        for interp in (False, True):
+            c = GPUConvolver(form=form)
+            c.update_sky(Sky(nss, *sky, None))
+            c.update_beam(beam)
+            c.set_interp(interp)
+            c.update_scan(Scan(n, ra, dec, pa))
+            a = np.zeros(n)
+            b = np.zeros(n)
+            c.exec_convolution(a, b)
+            out[form, interp] = (a, b)
+            c.close()
+    for interp, tol in ((False, 1e-6), (True, 1e-5)):
+        for x in range(2):
+            ref = out["fp64", interp][x]
+            d = out["tuned", interp][x] - ref
+            rms = np.sqrt(np.mean(ref ** 2))
+            assert np.sqrt(np.mean(d ** 2)) <= tol * rms, (interp, np.sqrt(np.mean(d ** 2)) / rms)
+            assert np.abs(d).max() <= tol * np.abs(ref).max(), (interp, np.abs(d).max() / rms)
