@@ -40,13 +40,15 @@ def _conv(form, sky, beam, ra, dec, pa, order, ptg=1 << 20):
     return c
 
 
+@pytest.mark.parametrize("bilinear", [False, True])
 @pytest.mark.parametrize("form", ["tuned", "plain", "fp64"])
-def test_sky_order_host_forward_bit_identical(gpu, form):
+def test_sky_order_host_forward_bit_identical(gpu, form, bilinear):
     sky, beam, ra, dec, pa = _inputs(3000, 11)
     out = {}
     for order in ("scan", "sky"):
         for ptg in (1 << 20, 700):  # one chunk, and chunks each sorted on their own
             c = _conv(form, sky, beam, ra, dec, pa, order, ptg)
+            c.set_interp(bilinear)
             a = np.zeros(len(ra), np.float64)
             b = np.zeros(len(ra), np.float64)
             c.exec_convolution(a, b)
