@@ -482,6 +482,18 @@ def run_c3_precision(args):
     t_tuned = e0.elapsed_time(e1) / 1e3
     tuned = [x.cpu().numpy() for x in out]
     fb = conv.last_fallbacks()
+    # the same forward in sky order (bit-identical TOD); the first launch sorts
+    conv.set_sample_order("sky")
+    so = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(2)]
+    conv.forward_device(so[0].data_ptr(), so[1].data_ptr(), out_f64=True, form="tuned", stream=cs)
+    conv.sync()
+    e0.record()
+    conv.forward_device(so[0].data_ptr(), so[1].data_ptr(), out_f64=True, form="tuned", stream=cs)
+    e1.record()
+    torch.cuda.synchronize()
+    t_sky = e0.elapsed_time(e1) / 1e3
+    sky_same = all(np.array_equal(a.cpu().numpy(), b) for a, b in zip(so, tuned))
+    conv.set_sample_order("scan")
     m = min(n, args.fp64_samples)
     ref = [torch.empty(m, dtype=torch.float64, device="cuda") for _ in range(2)]
     e0.record()
@@ -506,6 +518,8 @@ def run_c3_precision(args):
     errf = np.concatenate([ref[0][:mc] - oa, ref[1][:mc] - ob])
     line = {"workload": "c3_precision_nside2048_beam1deg", "nsamples": n, "pairs": pairs,
             "tuned_samples_per_s": n / t_tuned, "fp64_gpu_samples_per_s": m / t_fp64,
+            "tuned_sky_order": {"samples_per_s": n / t_sky, "over_scan_order": t_tuned / t_sky,
+                                "tod_bit_identical": sky_same},
             "fp64_fallback_pairs": fb, "worst_fp32_decision_error_over_margin": worst,
             "tuned_vs_fp64_gpu": {"rms": float(np.sqrt(np.mean(err ** 2)) / rms),
                                   "max": float(np.abs(err).max() / rms), "samples": m,
