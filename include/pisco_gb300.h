@@ -43,7 +43,12 @@ typedef enum pisco_dtype { PISCO_FLOAT32 = 0, PISCO_FLOAT64 = 1 } pisco_dtype;
  *        sky x beam products, FP64 accumulation).
  * TUNED: FP64 per-sample frame, FP32 per-pair geometry with an FP64
  *        re-evaluation of every decision that lies near a pixel edge, FP32
- *        products with compensated (two-sum) accumulation.
+ *        products with compensated (two-sum) accumulation.  With the
+ *        bilinear lookup the stencil is formed in FP32 and only pairs at the
+ *        boresight are re-evaluated (its weights are continuous).  A beam
+ *        whose disc reaches beyond the polar cap of its grid (rhoMax > 0.5
+ *        rad or within two rings of the cap's edge) is convolved by the
+ *        PLAIN chain instead.
  * FP64:  every input, product and sum in FP64. */
 typedef enum pisco_form {
     PISCO_FORM_PLAIN = 0,
