@@ -442,3 +442,46 @@ def test_wide_fine_beam_both_lookups(gpu, oracle_mod):
             rms = np.sqrt(np.mean(ref ** 2))
             assert np.sqrt(np.mean(d ** 2)) <= tol * rms, (interp, np.sqrt(np.mean(d ** 2)) / rms)
             assert np.abs(d).max() <= tol * np.abs(ref).max(), (interp, np.abs(d).max() / rms)
+
+
+def test_exact_and_near_pole_pointings(gpu, oracle_mod):
+    """Boresights exactly at the poles, one ulp on either side of them (the
+    frame flip of the TUNED geometry is decided there), and at dec = +-pi/2
+    given in float32: TUNED against the FP64 form with each lookup, and the
+    nearest lookup's disc exactly HEALPix's."""
+    from pisco4cmb_gb300 import GPUConvolver, PolBeam, Scan, Sky
+
+    nss, nsb = 128, 512
+    npb = oracle_mod.beam_npix_for_radius(nsb, np.deg2rad(3.0))
+    beam = PolBeam(nsb, npb, 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(1.3, 1.1, 15.0)
+    beam.build(nss)
+    hp = np.pi / 2
+    decs = [hp, -hp, np.nextafter(hp, 0), np.nextafter(-hp, 0), np.nextafter(hp, 4),
+            np.nextafter(-hp, -4), float(np.float32(hp)), float(np.float32(-hp)),
+            hp - 1e-9, -hp + 1e-9]
+    ras = [0.0, 1.0, np.pi, 5.5, 2 * np.pi, -0.3]
+    ra = np.array([r for r in ras for _ in decs])
+    dec = np.array([d for _ in ras for d in decs])
+    pa = np.linspace(0, 2 * np.pi, ra.size)
+    n = ra.size
+    sky = np.random.default_rng(3).normal(size=(3, 12 * nss * nss)).astype(np.float32)
+    out = {}
+    for form in ("tuned", "fp64"):
+        for interp in (False, True):
+            c = GPUConvolver(form=form)
+            c.update_sky(Sky(nss, *sky, None))
+            c.update_beam(beam)
+            c.set_interp(interp)
+            c.update_scan(Scan(n, ra, dec, pa))
+            a = np.zeros(n)
+            b = np.zeros(n)
+            c.exec_convolution(a, b)
+            out[form, interp] = (a, b)
+            if form == "tuned" and not interp:
+                worst, tp = c.tuned_calibrate(with_pairs=True)
+                assert tp == c.count_pairs() and worst < 0.5
+            c.close()
+    for interp, tol in ((False, 1e-6), (True, 1e-5)):
+        for x in range(2):
+            assert rel_max(out["tuned", interp][x], out["fp64", interp][x]) < tol, interp
