@@ -129,7 +129,6 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     const long long npix = 12LL * c->nside_sky * c->nside_sky;
     const long long nsky = 4 * npix, nbeam = 8LL * c->npix_beam;
-    const size_t osz = out_dtype == PISCO_FLOAT64 ? 8 : 4;
     AdjArgs a{};
     a.nside_sky = c->nside_sky;
     a.sky32 = c->sky32;
@@ -236,7 +235,6 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
                                      a.beam_scale > 0.0 ? 1.0 / a.beam_scale : 0.0, s),
                "beam gradient");
     }
-    (void)osz;
     if (s != c->stream) {
         cudaEvent_t ev;
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");

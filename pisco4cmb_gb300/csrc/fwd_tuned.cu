@@ -19,7 +19,7 @@ constexpr int kTW = PISCO_TUNED_WARPS;
 // kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
 template <bool kCalib, bool kBil>
 __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
-    tuned_kernel(FwdArgs a, float rscale, float* calib)
+    tuned_kernel(FwdArgs a, float* calib)
 {
     __shared__ tuned::WarpSmem sm[kTW];
     const int lane = threadIdx.x & 31;
@@ -27,7 +27,6 @@ __global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
     const Hpx hs = hpx_make(a.nside_sky);
     const Hpx hb = hpx_make(a.nside_beam);
     const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
-    (void)rscale;
     const long long gw = (long long)blockIdx.x * kTW + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kTW;
     unsigned long long nfall = 0, npairs = 0;
@@ -92,18 +91,17 @@ cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, f
 {
     if (a.n <= 0) return cudaSuccess;
     const int threads = kTW * 32;
-    const float rscale = (float)(1.7320508075688772 * (double)a.nside_beam);
     const long long need = (a.n + kTW - 1) / kTW;
     // calibration measures the nearest-pixel decisions, whatever the lookup
     if (calib) {
         long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<true, false>, threads);
-        tuned_kernel<true, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, calib);
+        tuned_kernel<true, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, calib);
     } else if (a.interp == 1) {
         long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, true>, threads);
-        tuned_kernel<false, true><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, nullptr);
+        tuned_kernel<false, true><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, nullptr);
     } else {
         long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, false>, threads);
-        tuned_kernel<false, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, rscale, nullptr);
+        tuned_kernel<false, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, nullptr);
     }
     return cudaGetLastError();
 }
