@@ -1,7 +1,7 @@
 #!/bin/sh
 # Builds oracle/_ref/ (TEST INFRASTRUCTURE ONLY) from the reference's own
 # sources, read in place from the reference tree ($PISCO_REFERENCE, default
-# /root/reference).  Nothing from the reference tree is copied; outputs go to
+# the directory "reference" beside this repository).  Nothing from the reference tree is copied; outputs go to
 # oracle/_ref/ only (git-ignored).
 #   libpisco_ref.so    : Convolver, Sky, Scan, PolBeam, Sphtrigo compiled
 #                        unmodified with the reference's CPU flags
@@ -19,7 +19,7 @@
 #                        by oracle/ref_gpu_harness.cpp.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${PISCO_REFERENCE:-/root/reference}
+REF=${PISCO_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
 CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
 if [ ! -f "$REF/src/Convolver/convolver.cpp" ]; then

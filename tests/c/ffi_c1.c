@@ -83,7 +83,7 @@ int main(int argc, char** argv)
     st = pisco_beam_build(nsb, npb, 0.01, 'p', nside, ta, tb, oa, ob);
     if (st != PISCO_OK) return fail("beam build", st, NULL);
 
-    /* convolver: the INTEGRATION.md sequence */
+    /* convolver: create, set sky / beam / scan, forward, destroy */
     pisco_run_config cfg = {1, 0, 0, 0, 0, 0, 0, 1 << 20, 0};
     pisco_ctx* ctx = NULL;
     st = pisco_create(&cfg, &ctx);

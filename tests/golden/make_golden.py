@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own code.
 
-Needs the reference tree (PISCO_REFERENCE, default /root/reference) to build
+Needs the reference tree (PISCO_REFERENCE, default: the directory "reference" beside this repository) to build
 oracle/_ref (see oracle/build_ref.sh).  Outputs, all small .npz files:
 
 * golden_c1.npz      -- the CPU-runnable workload (sky nside 64 float64 I,Q,U;

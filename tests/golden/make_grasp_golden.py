@@ -3,7 +3,7 @@ ingest scripts on seeded synthetic GRASP uv-grids.
 
 The scripts (scripts/fields2beams.py, scripts/fields2beams_cxisco.py and
 scripts/graspbeam_to_healpix.py of the reference tree, PISCO_REFERENCE,
-default /root/reference) are executed unmodified with runpy.  Two modules they
+default: the directory "reference" beside this repository) are executed unmodified with runpy.  Two modules they
 import are absent here and are stood in for:
 
 * healpy: ``ang2pix``/``pix2ang`` come from the reference's own HEALPix port
@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 import oracle as O  # noqa: E402
 from pisco4cmb_gb300 import io as pio  # noqa: E402
 
-REF = os.environ.get("PISCO_REFERENCE", "/root/reference")
+REF = os.environ.get("PISCO_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 NSIDE = 256
 
 
