@@ -163,6 +163,40 @@ def make_workload(device: str, nsamples: int, shard: int = 0, nshards: int = 1):
                 gen_s=time.time() - t0)
 
 
+class _Planes:
+    """Beam planes of the reference arm (PolBeam::aBeams / bBeams)."""
+
+    def __init__(self, nside, a, b):
+        self.nside, self._a, self._b = nside, a, b
+
+    def planes(self):
+        return self._a, self._b
+
+
+def make_reference_workload(device: str, nsamples: int):
+    """The workload of make_workload built without libpisco_gb300: the beam by
+    the reference's own PolBeam (oracle/_ref), else by the oracle's
+    restatement of it (bit-identical to the reference's, tested)."""
+    import oracle
+    from pisco4cmb_gb300 import synth
+
+    w = synth.WORKLOADS[2]
+    t0 = time.time()
+    sky = synth.grf_sky(w["nside_sky"], 2, dtype=np.float32, device=device)
+    nsb = w["nside_beam"]
+    npb = oracle.beam_npix_for_radius(nsb, math.radians(w["radius_deg"]))
+    fx, fy = synth.elliptical_fwhm(w["fwhm_deg"], w["ellipticity"])
+    if oracle.ref_available():
+        ba, bb, _ = oracle.ref_gaussian_beams(nsb, npb, fx, fy, 0.0, w["epsilon"], w["nside_sky"])
+        beam_by = "reference PolBeam (oracle/_ref)"
+    else:
+        ba, bb = oracle.gaussian_beams(nsb, npb, fx, fy, 0.0, w["epsilon"], w["nside_sky"])
+        beam_by = "oracle PolBeam restatement"
+    ra, dec, psi = synth.sweep_scan(nsamples, 2)
+    return dict(sky=sky, beam=_Planes(nsb, ba, bb), ra=ra, dec=dec, pa=psi,
+                nside_sky=w["nside_sky"], gen_s=time.time() - t0, beam_by=beam_by)
+
+
 # ------------------------------------------------------------------ CPU arm
 def cpu_forward(wl, n: int, threads: int, prefer_ref: bool = True):
     """(kind, seconds, tod_a) of the CPU implementation on the first n samples."""
@@ -209,7 +243,7 @@ def run_reference_arm(args, rank, world):
         gen_dev = "cuda" if torch.cuda.is_available() else "cpu"
     except Exception:  # noqa: BLE001
         gen_dev = "cpu"
-    wl = make_workload(gen_dev, 200_000)
+    wl = make_reference_workload(gen_dev, 200_000)
     threads = host_cores()
     n, kind = cpu_sample_size(wl, threads, 5.0)
     for _ in range(args.warmup):
@@ -663,6 +697,21 @@ def run_c5_adjoint(args):
                     ga.data_ptr(), gb.data_ptr(), False, gsky.data_ptr(),
                     gbeam.data_ptr() if with_beam else 0, deterministic=det, stream=cs,
                     sky_iqu=iqu))
+    # the fused beam-parameter gradient (no beam-map gradient): the model beam
+    # on the device, then sky (I, Q, U) + parameter gradients in one adjoint
+    params = (w["fwhm_deg"], w["ellipticity"], 0.0, 0.0, 0.0)
+    ab = torch.empty((beam.nPixels, 8), device="cuda")
+    conv.gaussian_beam_device(nsb, beam.nPixels, w["epsilon"], nss, *params, ab.data_ptr(),
+                              set_beam=True)
+    grad = torch.empty(5, dtype=torch.float64, device="cuda")
+    for det in (True, False):
+        for with_sky in (True, False):
+            key = (("deterministic" if det else "atomic") +
+                   ("_sky_iqu_and_params_fused" if with_sky else "_params_fused"))
+            res[key] = timeit(lambda: conv.adjoint_gaussian_device(
+                ga.data_ptr(), gb.data_ptr(), False, gsky.data_ptr() if with_sky else 0,
+                grad.data_ptr(), params, w["epsilon"], nss, deterministic=det, stream=cs,
+                sky_iqu=True))
     line = {"workload": "c5_adjoint_nside256_beam4deg", "nsamples": n, "pairs": pairs,
             "forward_ms": t_fwd * 1e3,
             "adjoint_ms": {k: v * 1e3 for k, v in res.items()},

@@ -6,7 +6,10 @@
 // exec_convolution(data_a, data_b) computes both detectors.  Differences on
 // purpose: every sample is computed (the reference drops the tail,
 // gpuconvolver.cu:386); CUDA failures throw std::runtime_error instead of
-// exit(-1); set_form() selects the PLAIN (default), TUNED or FP64 form.
+// exit(-1); the default form is TUNED (FP32 per-pair geometry with FP64
+// pointing and an FP64 re-evaluation of every near-edge pixel decision; a
+// beam outside its domain is convolved by the PLAIN chain automatically);
+// set_form() selects PLAIN (the reference's per-pair chain), TUNED or FP64.
 #ifndef PISCO_GPUCONVOLVER_HPP
 #define PISCO_GPUCONVOLVER_HPP
 
@@ -21,7 +24,7 @@
 
 class GPUConvolver {
   public:
-    explicit GPUConvolver(CUDACONV::RunConfig cfg_) : ctx(nullptr), nsamples(0), form(PISCO_FORM_PLAIN)
+    explicit GPUConvolver(CUDACONV::RunConfig cfg_) : ctx(nullptr), nsamples(0), form(PISCO_FORM_TUNED)
     {
         std::memcpy(&cfg, &cfg_, sizeof(cfg));
     }

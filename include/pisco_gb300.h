@@ -156,6 +156,56 @@ pisco_status pisco_last_fallbacks(pisco_ctx* ctx, long long* fallbacks);
 pisco_status pisco_tuned_calibrate(pisco_ctx* ctx, long begin, long n, double* worst_fraction,
                                    long long* tuned_pairs);
 
+/* ---- per-pair record of a form's decisions (diagnostic; no reference
+ *      counterpart as an entry point -- the reference checks the same
+ *      decisions in its device tests, tests/cudaConvolution/
+ *      test_sky_to_beam_matching_kernel.cu:188-216) ---------------------- */
+/* Host arrays of `capacity` entries each (4 per entry for the stencil);
+ * any pointer may be NULL (that field is not returned). */
+typedef struct pisco_pair_dump {
+    long long capacity;
+    int* sample;       /* position of the pair's sample in [0, n) */
+    int* sky_pix;      /* the disc pixel (RING) */
+    int* beam_pix;     /* nearest lookup: the beam pixel chosen, also when it
+                          lies beyond the stored map; bilinear lookup: -1 */
+    float* c2chi;      /* cos 2chi and sin 2chi as the form multiplies by them */
+    float* s2chi;
+    double* chi;       /* PLAIN / FP64: the FP64 chi; TUNED: NaN */
+    int* flags;        /* PISCO_PAIR_REDONE | PISCO_PAIR_OUTSIDE_BEAM */
+    int* stencil_pix;  /* bilinear lookup: 4 stencil pixels per pair, in
+                          get_interpol's order; nearest: -1 */
+    double* stencil_w; /* TUNED: the FP32 weights the kernel multiplies by
+                          (renormalised over the stored map, 0 beyond it);
+                          PLAIN / FP64: get_interpol's FP64 weights */
+} pisco_pair_dump;
+#define PISCO_PAIR_REDONE 1       /* TUNED: re-evaluated with the FP64 chain */
+#define PISCO_PAIR_OUTSIDE_BEAM 2 /* beam pixel (every stencil pixel) beyond the
+                                     stored map: the pair adds nothing */
+/* Runs the per-sample body of `form` (with the context's beam lookup) over
+ * samples [begin, begin+n) of the current scan and records every (sample,
+ * disc pixel) pair it visits: each sample's pairs appear together, in no
+ * particular order within the sample.  *npairs = the number of disc pairs of
+ * the range (HEALPix query_disc).  out == NULL only sizes the record;
+ * out->capacity below *npairs is PISCO_ERR_INVALID_ARGUMENT.  Synchronous;
+ * allocates its device buffers for the call. */
+pisco_status pisco_debug_pairs(pisco_ctx* ctx, pisco_form form, long begin, long n,
+                               const pisco_pair_dump* out, long long* npairs);
+
+/* ---- HEALPix RING on the device, whole arrays (the device routines every
+ *      kernel uses; the reference's device port is
+ *      src/GpuConvolver/cuda/cudaHealpix.cu:56-259) ---------------------
+ * Device arrays of n values on `stream` (NULL: the legacy default stream)
+ * of the current device; synchronous.  An out-of-range input is
+ * PISCO_ERR_INVALID_ARGUMENT (its outputs are NaN / -1). */
+pisco_status pisco_hpx_pix2ang_device(int nside, long long n, const long long* d_pix,
+                                      double* d_theta, double* d_phi, void* stream);
+pisco_status pisco_hpx_ang2pix_device(int nside, long long n, const double* d_theta,
+                                      const double* d_phi, long long* d_pix, void* stream);
+/* Four pixels and weights per point (n x 4 each), get_interpol's order. */
+pisco_status pisco_hpx_get_interpol_device(int nside, long long n, const double* d_theta,
+                                           const double* d_phi, long long* d_pix4, double* d_w4,
+                                           void* stream);
+
 /* ---- batched multi-detector forward ------------------------------------ */
 /* One detector pair of a batched forward.  Device pointers: FP64 pointing
  * of nsamples samples and the two TOD outputs (out_dtype; either may be
@@ -209,8 +259,11 @@ pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, 
  * PISCO_NOALLOC_MAX_ITEMS work items, sum over pairs of
  * ceil(nsamples / chunk) -- raise chunk for long scans; beyond either limit
  * the call returns PISCO_ERR_INVALID_ARGUMENT with the reason in
- * pisco_last_error(NULL).  The first call on a device looks up the array's
- * device address and should come before any stream capture on that device.
+ * pisco_last_error(NULL); so does a pair of more than 2^40 samples.  The
+ * first call on a device looks up the array's device address and should
+ * come before any stream capture on that device; the address is kept for
+ * the life of the process, so do not call this entry point on a device
+ * after a cudaDeviceReset of it.
  * Calls whose GPU work overlaps race on the shared array: serialise them. */
 #define PISCO_NOALLOC_MAX_DETS 128
 #define PISCO_NOALLOC_MAX_ITEMS 32768
@@ -218,7 +271,7 @@ pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, 
 typedef struct pisco_noalloc_det {
     int nside_beam;
     long npix_beam;
-    const float* beam_ab; /* device, npix_beam x 8: a.I,Q,U,V, b.I,Q,U,V; 16-B aligned */
+    const float* beam_ab; /* device, npix_beam x 8: a.I,Q,U,V, b.I,Q,U,V; 32-B aligned */
     long long nsamples;
     const double* ra; /* device FP64 pointing */
     const double* dec;
@@ -259,6 +312,23 @@ pisco_status pisco_adjoint_device(pisco_ctx* ctx, long begin, long n, const void
                                   const void* d_gb, pisco_dtype g_dtype, void* d_gsky,
                                   void* d_gbeam, pisco_dtype out_dtype, pisco_adjoint_mode mode,
                                   void* stream);
+/* The adjoint with the beam-parameter gradient formed directly (no
+ * reference counterpart): for a context whose beam is the elliptical
+ * Gaussian pair model of pisco_beam_gaussian_device with these parameters,
+ * d_grad (5 device doubles) = dL/d(fwhm_deg, ellipticity, phi0_deg, dx, dy),
+ * the value pisco_beam_gaussian_param_grad_device gives from
+ * pisco_adjoint_device's beam-map gradient, without forming that map: each
+ * pair's share is weighted by the model's weight and derivatives, recomputed
+ * from the parameters for every call at the beam pixel centres, and reduced
+ * per warp and then in warp order (the same result on every run, in either
+ * mode).  d_gsky as pisco_adjoint_device (may be NULL); the mode selects the
+ * sky gradient's accumulation. */
+pisco_status pisco_adjoint_gaussian_device(pisco_ctx* ctx, long begin, long n, const void* d_ga,
+                                           const void* d_gb, pisco_dtype g_dtype, void* d_gsky,
+                                           pisco_dtype out_dtype, pisco_adjoint_mode mode,
+                                           double epsilon, int nside_sky, double fwhm_deg,
+                                           double ellipticity, double phi0_deg, double dx,
+                                           double dy, double* d_grad, void* stream);
 /* Host arrays: g_a, g_b (nsamples each) in; sky gradient planes out (any of
  * gI, gQ, gU, gV may be NULL). */
 pisco_status pisco_adjoint(pisco_ctx* ctx, const void* g_a, const void* g_b, pisco_dtype g_dtype,

@@ -1,8 +1,12 @@
 #!/bin/sh
 # Builds oracle/_ref/ (TEST INFRASTRUCTURE ONLY) from the reference's own
-# sources, read in place from the reference tree ($PISCO_REFERENCE, default
-# the directory "reference" beside this repository).  Nothing from the reference tree is copied; outputs go to
-# oracle/_ref/ only (git-ignored).
+# sources: the reference tree ($PISCO_REFERENCE, default the directory
+# "reference" beside this repository) when it is present, else the copy of
+# its src/ folder that an earlier run on a machine with the tree staged in
+# oracle/_ref/src_tree/.  Everything under oracle/_ref/ is git-ignored and
+# never committed: the staged copy only lets a machine without the reference
+# tree (and of another architecture) compile the reference's own code
+# itself.  Outputs go to oracle/_ref/ only.
 #   libpisco_ref.so    : Convolver, Sky, Scan, PolBeam, Sphtrigo compiled
 #                        unmodified with the reference's CPU flags
 #                        (CMakeLists.txt:27,37-39) against the HEALPix shim
@@ -21,9 +25,19 @@ set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${PISCO_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
+STAGE="$OUT/src_tree"
 CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
-if [ ! -f "$REF/src/Convolver/convolver.cpp" ]; then
-    echo "build_ref.sh: reference tree not found at $REF; skipping" >&2
+if [ -f "$REF/src/Convolver/convolver.cpp" ]; then
+    # only the folders this recipe compiles (about 170 KB)
+    rm -rf "$STAGE"
+    mkdir -p "$STAGE/src"
+    for d in Convolver Sky Scan Polbeam Sphtrigo SkyMap GpuConvolver; do
+        cp -R "$REF/src/$d" "$STAGE/src/$d"
+    done
+elif [ -f "$STAGE/src/Convolver/convolver.cpp" ]; then
+    REF="$STAGE"
+else
+    echo "build_ref.sh: reference tree not found at $REF and no staged copy; skipping" >&2
     exit 0
 fi
 mkdir -p "$OUT/obj"

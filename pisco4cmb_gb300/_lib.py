@@ -80,6 +80,19 @@ class NoallocDet(ctypes.Structure):
                 ("tod_a", ctypes.c_void_p), ("tod_b", ctypes.c_void_p)]
 
 
+class PairDump(ctypes.Structure):
+    """pisco_pair_dump: host arrays receiving a form's per-pair decisions."""
+
+    _fields_ = [("capacity", ctypes.c_longlong), ("sample", ctypes.c_void_p),
+                ("sky_pix", ctypes.c_void_p), ("beam_pix", ctypes.c_void_p),
+                ("c2chi", ctypes.c_void_p), ("s2chi", ctypes.c_void_p), ("chi", ctypes.c_void_p),
+                ("flags", ctypes.c_void_p), ("stencil_pix", ctypes.c_void_p),
+                ("stencil_w", ctypes.c_void_p)]
+
+
+PAIR_REDONE = 1
+PAIR_OUTSIDE_BEAM = 2
+
 NOALLOC_MAX_DETS = 128
 NOALLOC_MAX_ITEMS = 32768
 
@@ -111,6 +124,11 @@ SIGNATURES = [
     ("pisco_last_fallbacks", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_longlong)]),
+    ("pisco_debug_pairs", _S, [_P, _I, _L, _L, ctypes.POINTER(PairDump),
+                               ctypes.POINTER(ctypes.c_longlong)]),
+    ("pisco_hpx_pix2ang_device", _S, [_I, ctypes.c_longlong, _P, _P, _P, _P]),
+    ("pisco_hpx_ang2pix_device", _S, [_I, ctypes.c_longlong, _P, _P, _P, _P]),
+    ("pisco_hpx_get_interpol_device", _S, [_I, ctypes.c_longlong, _P, _P, _P, _P, _P]),
     ("pisco_set_beam_slot", _S, [_P, _I, _I, _L, _PP, _PP, _I]),
     ("pisco_forward_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, _I, _P]),
     ("pisco_autotune_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, ctypes.c_char_p,
@@ -119,6 +137,8 @@ SIGNATURES = [
     ("pisco_set_beam_device", _S, [_P, _I, _L, _P, _I, _P]),
     ("pisco_adjoint_device", _S, [_P, _L, _L, _P, _P, _I, _P, _P, _I, _I, _P]),
     ("pisco_adjoint", _S, [_P, _P, _P, _I, _P, _P, _P, _P, _I, _I]),
+    ("pisco_adjoint_gaussian_device", _S, [_P, _L, _L, _P, _P, _I, _P, _I, _I, _D, _I, _D, _D,
+                                           _D, _D, _D, _P, _P]),
     ("pisco_hpx_pix2ang", _S, [_I, _L, _P, _P, _P]),
     ("pisco_hpx_ang2pix", _S, [_I, _L, _P, _P, _P]),
     ("pisco_beam_npix_for_radius", _L, [_I, _D]),

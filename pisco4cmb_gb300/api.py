@@ -211,11 +211,13 @@ class PolBeam:
 class GPUConvolver:
     """Drop-in for the reference GPUConvolver on one GB300.
 
-    ``form``: "plain" (the reference chain), "tuned" (FP32 per-pair geometry
-    with FP64 re-evaluation near pixel edges) or "fp64".
+    ``form``: "tuned" (the default: FP32 per-pair geometry with FP64
+    pointing and FP64 re-evaluation near pixel edges; a beam outside its
+    domain is convolved by the PLAIN chain automatically), "plain" (the
+    reference chain) or "fp64".
     """
 
-    def __init__(self, cfg: RunConfig | None = None, form: str = "plain"):
+    def __init__(self, cfg: RunConfig | None = None, form: str = "tuned"):
         self.cfg = cfg if cfg is not None else RunConfig()
         self.form = form
         if form not in FORMS:
@@ -386,6 +388,23 @@ class GPUConvolver:
                                           mode, stream or None),
               self.ctx, "adjoint_device")
 
+    def adjoint_gaussian_device(self, d_ga: int, d_gb: int, g_f64: bool, d_gsky: int,
+                                d_grad: int, params, epsilon: float, nside_sky: int,
+                                out_f64: bool = False, deterministic: bool = True, begin: int = 0,
+                                n: int | None = None, stream: int = 0,
+                                sky_iqu: bool = False) -> None:
+        """Adjoint with the Gaussian beam-parameter gradient formed directly:
+        d_grad (5 device doubles) = dL/d(fwhm_deg, ellipticity, phi0_deg, dx,
+        dy) for a context whose beam is that model (gaussian_beam_device with
+        ``params``); d_gsky (may be 0) as adjoint_device."""
+        n = self._n - begin if n is None else n
+        mode = (1 if deterministic else 0) | (2 if sky_iqu else 0)
+        f, e, p0, dx, dy = (float(v) for v in params)
+        check(load().pisco_adjoint_gaussian_device(
+            self.ctx, begin, n, d_ga, d_gb, FLOAT64 if g_f64 else FLOAT32, d_gsky or None,
+            FLOAT64 if out_f64 else FLOAT32, mode, float(epsilon), int(nside_sky), f, e, p0, dx,
+            dy, d_grad, stream or None), self.ctx, "adjoint_gaussian_device")
+
     def adjoint(self, g_a: np.ndarray, g_b: np.ndarray, deterministic: bool = True,
                 out_f64: bool = True):
         """Host-array adjoint: returns dL/d(I, Q, U, V) as a 4 x npix array."""
@@ -443,6 +462,30 @@ class GPUConvolver:
         check(load().pisco_tuned_calibrate(self.ctx, begin, n, ctypes.byref(v), ctypes.byref(p)),
               self.ctx, "tuned_calibrate")
         return (float(v.value), int(p.value)) if with_pairs else float(v.value)
+
+    def debug_pairs(self, form: str | None = None, begin: int = 0, n: int | None = None) -> dict:
+        """Every (sample, disc pixel) pair the kernels of ``form`` visit over
+        samples [begin, begin+n), with their decisions (pisco_debug_pairs):
+        a dict of numpy arrays, sorted by (sample, sky pixel)."""
+        n = self._n - begin if n is None else n
+        L = load()
+        f = FORMS[form or self.form]
+        tot = ctypes.c_longlong()
+        check(L.pisco_debug_pairs(self.ctx, f, begin, n, None, ctypes.byref(tot)), self.ctx,
+              "debug_pairs")
+        m = int(tot.value)
+        out = dict(sample=np.empty(m, np.int32), sky_pix=np.empty(m, np.int32),
+                   beam_pix=np.empty(m, np.int32), c2chi=np.empty(m, np.float32),
+                   s2chi=np.empty(m, np.float32), chi=np.empty(m, np.float64),
+                   flags=np.empty(m, np.int32), stencil_pix=np.empty((m, 4), np.int32),
+                   stencil_w=np.empty((m, 4), np.float64))
+        rec = _lib.PairDump(m, *[_ptr(out[k]) for k in ("sample", "sky_pix", "beam_pix", "c2chi",
+                                                       "s2chi", "chi", "flags", "stencil_pix",
+                                                       "stencil_w")])
+        check(L.pisco_debug_pairs(self.ctx, f, begin, n, ctypes.byref(rec), ctypes.byref(tot)),
+              self.ctx, "debug_pairs")
+        order = np.lexsort((out["sky_pix"], out["sample"]))
+        return {k: v[order] for k, v in out.items()}
 
     def last_fallbacks(self) -> int:
         v = ctypes.c_longlong()

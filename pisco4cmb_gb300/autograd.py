@@ -13,7 +13,11 @@ No per-pair weights are stored.  ``gaussian_beam`` is the same model as a
 ``torch.autograd.Function`` on the library's kernels (beam built on the GPU
 by ``pisco_beam_gaussian_device``, gradient reduced by
 ``pisco_beam_gaussian_param_grad_device``), for fitting loops that should not
-run the beam through torch operations.
+run the beam through torch operations.  ``convolve_gaussian(sky, params,
+conv, ...)`` goes one step further: its backward forms dL/dparams inside the
+adjoint (``pisco_adjoint_gaussian_device``), weighting each pair by the
+model's weight and derivatives recomputed at its beam pixel, so no beam-map
+gradient is accumulated at all.
 """
 from __future__ import annotations
 
@@ -24,8 +28,8 @@ import torch
 
 from .api import GPUConvolver, pix2ang
 
-__all__ = ["convolve", "gaussian_polbeam", "gaussian_beam", "beam_pixel_coords", "ConvolveFn",
-           "GaussianBeamFn"]
+__all__ = ["convolve", "convolve_gaussian", "gaussian_polbeam", "gaussian_beam",
+           "beam_pixel_coords", "ConvolveFn", "ConvolveGaussianFn", "GaussianBeamFn"]
 
 
 def _torch_stream(device=None) -> int:
@@ -190,6 +194,77 @@ class GaussianBeamFn(torch.autograd.Function):
                                                  g.data_ptr(), g.dtype == torch.float64,
                                                  out.data_ptr(), stream=stream)
         return out.to(device=pdev, dtype=dtype), None, None, None, None, None
+
+
+class ConvolveGaussianFn(torch.autograd.Function):
+    """TOD (a, b) of a sky and the elliptical Gaussian pair beam of params =
+    (fwhm_deg, ellipticity, phi0_deg, dx, dy), the beam built on the GPU.
+    The backward forms dL/dparams in the adjoint itself
+    (pisco_adjoint_gaussian_device): the model's weights and derivatives are
+    recomputed from the parameters at the beam pixels, and no beam-map
+    gradient is formed."""
+
+    @staticmethod
+    def forward(ctx, sky, params, conv: GPUConvolver, nside_sky: int, nside_beam: int, npix: int,
+                epsilon: float, deterministic: bool):
+        if not sky.is_cuda:
+            raise ValueError("sky must be a CUDA tensor")
+        if params.numel() != 5:
+            raise ValueError("params must hold (fwhm_deg, ellipticity, phi0_deg, dx, dy)")
+        p = [float(v) for v in params.detach().double().cpu().tolist()]
+        sky4 = _as_iquv(sky)
+        stream = _torch_stream(sky.device)
+        bab = torch.empty((int(npix), 8), dtype=torch.float32, device=sky.device)
+        conv.set_sky_device(nside_sky, sky4.data_ptr(), False, stream=stream)
+        conv.gaussian_beam_device(nside_beam, npix, epsilon, nside_sky, *p, bab.data_ptr(),
+                                  set_beam=True, stream=stream)
+        n = conv._n
+        out_dt = torch.float64 if sky.dtype == torch.float64 else torch.float32
+        ta = torch.empty(n, dtype=out_dt, device=sky.device)
+        tb = torch.empty(n, dtype=out_dt, device=sky.device)
+        conv.forward_device(ta.data_ptr(), tb.data_ptr(), out_f64=out_dt == torch.float64,
+                            stream=stream, form="tuned")
+        ctx.save_for_backward(sky4, bab)
+        ctx.conv = conv
+        ctx.meta = (nside_sky, nside_beam, int(npix), float(epsilon), deterministic, p,
+                    sky.shape, sky.dtype, params.dtype, params.device)
+        return ta, tb
+
+    @staticmethod
+    def backward(ctx, ga, gb):
+        sky4, bab = ctx.saved_tensors
+        conv = ctx.conv
+        nside_sky, nside_beam, npix, eps, det, p, sky_shape, sky_dtype, pdt, pdev = ctx.meta
+        stream = _torch_stream(sky4.device)
+        conv.set_sky_device(nside_sky, sky4.data_ptr(), False, stream=stream)
+        conv.set_beam_device(nside_beam, npix, bab.data_ptr(), False, stream=stream)
+        n = conv._n
+        ga = (ga if ga is not None else torch.zeros(n, device=sky4.device)).contiguous()
+        gb = (gb if gb is not None else torch.zeros(n, device=sky4.device)).contiguous()
+        g64 = ga.dtype == torch.float64
+        gb = gb.to(ga.dtype)
+        want_sky = ctx.needs_input_grad[0]
+        gsky = torch.empty((sky4.shape[0], 4), dtype=torch.float64, device=sky4.device) if want_sky else None
+        grad = torch.empty(5, dtype=torch.float64, device=sky4.device)
+        iqu = len(sky_shape) == 2 and 3 in tuple(sky_shape)
+        conv.adjoint_gaussian_device(ga.data_ptr(), gb.data_ptr(), g64,
+                                     gsky.data_ptr() if gsky is not None else 0, grad.data_ptr(),
+                                     p, eps, nside_sky, out_f64=True, deterministic=det,
+                                     stream=stream, sky_iqu=iqu)
+        if gsky is not None:
+            gsky = _like_sky(gsky, sky_shape).to(sky_dtype)
+        gp = grad.to(device=pdev, dtype=pdt) if ctx.needs_input_grad[1] else None
+        return gsky, gp, None, None, None, None, None, None
+
+
+def convolve_gaussian(sky: torch.Tensor, params: torch.Tensor, conv: GPUConvolver, nside_sky: int,
+                      nside_beam: int, npix: int, epsilon: float = 0.01,
+                      deterministic: bool = True):
+    """Differentiable TUNED forward with the Gaussian pair beam of ``params``
+    (fwhm_deg, ellipticity, phi0_deg, dx, dy): returns (tod_a, tod_b); the
+    parameter gradient comes from the fused adjoint."""
+    return ConvolveGaussianFn.apply(sky, params, conv, nside_sky, nside_beam, npix, epsilon,
+                                    deterministic)
 
 
 def gaussian_beam(params: torch.Tensor, conv: GPUConvolver, nside_beam: int, npix: int,

@@ -23,6 +23,8 @@
 //    per-pixel error is at most (#contributions x 2^-S) / 2.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "tuned_core.cuh"
 
 namespace pisco {
@@ -55,13 +57,13 @@ struct Scatter {
         p.ga = ga;
         p.gb = gb;
     }
-    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, float c2,
-                                            float s2, float&, float&) const
+    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, int,
+                                            float c2, float s2, float&, float&) const
     {
         scatter(p.ga, p.gb, pix, B, c2, s2);
     }
     __device__ __forceinline__ int fetch(int) const { return 0; }
-    __device__ __forceinline__ void pair(int pix, int, const F8& B, float c2, float s2) const
+    __device__ __forceinline__ void pair(int pix, int, const F8& B, int, float c2, float s2) const
     {
         scatter(ga, gb, pix, B, c2, s2);
     }
@@ -85,10 +87,10 @@ struct Scatter {
     }
 };
 
-// Sky and beam gradient: with the nearest lookup the beam pixel index is
-// recovered as &B - base (the action receives a reference to beam[bp]
-// itself); with the bilinear one the action gets the stencil and spreads
-// each pair's beam gradient over its (up to) four pixels by their weights.
+// Sky and beam gradient: with the nearest lookup the action gets the beam
+// pixel bp with its value; with the bilinear one it gets the stencil and
+// spreads each pair's beam gradient over its (up to) four pixels by their
+// weights.
 template <bool kFixed>
 struct ScatterBeam {
     static constexpr bool kSums = false;
@@ -109,16 +111,16 @@ struct ScatterBeam {
         p.ga = ga;
         p.gb = gb;
     }
-    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, float c2,
-                                            float s2, float&, float&) const
+    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, int bp,
+                                            float c2, float s2, float&, float&) const
     {
-        scatter(p.ga, p.gb, pix, fetch(pix), B, c2, s2);
+        scatter(p.ga, p.gb, pix, fetch(pix), B, bp, c2, s2);
     }
     __device__ __forceinline__ float4 fetch(int pix) const { return __ldg(&sky[pix]); }
-    __device__ __forceinline__ void pair(int pix, const float4& S, const F8& B, float c2,
+    __device__ __forceinline__ void pair(int pix, const float4& S, const F8& B, int bp, float c2,
                                          float s2) const
     {
-        scatter(ga, gb, pix, S, B, c2, s2);
+        scatter(ga, gb, pix, S, B, bp, c2, s2);
     }
 
     __device__ __forceinline__ void pair_stencil(int pix, const float4& S, const int px[4],
@@ -154,7 +156,7 @@ struct ScatterBeam {
     }
 
     __device__ __forceinline__ void scatter(float wa, float wb, int pix, const float4& S,
-                                           const F8& B, float c2, float s2) const
+                                           const F8& B, long long bp, float c2, float s2) const
     {
         if (want_sky) {
             const Scatter<kFixed> sc{wa,      wb,   gsky,  gsky_fx, nullptr,
@@ -163,7 +165,6 @@ struct ScatterBeam {
         }
         float v[8];
         beam_grad(wa, wb, S, c2, s2, v);
-        const long long bp = &B - beam_base;
         if (kFixed) {
             unsigned long long* p = gbeam_fx + 8 * bp;
 #pragma unroll
@@ -189,7 +190,7 @@ struct ScatterBeam {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 if (w[i] == 0.0f) continue;
-                const F8 v = beam_base[px[i]];
+                const F8 v = tuned::load_beam(beam_base + px[i]);
                 B.a.x = fmaf(v.a.x, w[i], B.a.x); B.a.y = fmaf(v.a.y, w[i], B.a.y);
                 B.a.z = fmaf(v.a.z, w[i], B.a.z); B.a.w = fmaf(v.a.w, w[i], B.a.w);
                 B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);
@@ -206,6 +207,113 @@ struct ScatterBeam {
             if (w[i] != 0.0f) add_beam(px[i], v, w[i]);
     }
 };
+
+// Sky gradient (optional) and the beam-parameter gradient of the elliptical
+// Gaussian pair model, without a beam-map gradient.  The model beam is
+// B[b] = c g[b] / N with c = (1 + eps, 1 - eps, 0, 0) for both detectors
+// (beam_model.h), so a pair's share of dL/dB[b] . dB[b]/dt needs only
+//   s = (1 + eps)(ga + gb) I + (1 - eps)(ga - gb)(Q cos 2chi + U sin 2chi),
+// its TOD weights times c . dtod/dB: each lane adds s g[b] and s dg[b]/dt
+// (t = F, e, phi0, dx, dy), read from the per-pixel table the adjoint entry
+// point recomputes from the parameters, into six compensated FP32 sums.  The
+// warp's sums are written to its own row of ppart (FP64, fixed shuffle
+// tree); launch_fold_params adds the rows in warp order, so the result is
+// the same on every run.  With the bilinear lookup the pair's beam value is
+// sum_i w_i B[b_i], and each stencil pixel gets w_i of s.
+template <bool kFixed>
+struct ScatterParams {
+    static constexpr bool kSums = false;
+    static constexpr bool kStencil = true;
+    float ga, gb;
+    const F8* beam_base;
+    const float4* sky;
+    const F8* ptab;
+    double* ppart;
+    float ci, cq;  // 1 + eps, 1 - eps
+    Scatter<kFixed> sc;
+    int want_sky;
+    float acc[6], cmp[6];
+
+    __device__ __forceinline__ void stash(tuned::Pend& p) const
+    {
+        p.ga = ga;
+        p.gb = gb;
+    }
+    __device__ __forceinline__ float4 fetch(int pix) const { return __ldg(&sky[pix]); }
+    __device__ __forceinline__ void add(float wa, float wb, const float4& S, float c2, float s2,
+                                        int b, float w)
+    {
+        const float qa = fmaf(S.y, c2, S.z * s2);
+        const float sp = w * fmaf(ci * (wa + wb), S.x, cq * (wa - wb) * qa);
+        const F8 t = tuned::load_beam(ptab + b);
+        tuned::two_sum(acc[0], cmp[0], sp * t.a.x);
+        tuned::two_sum(acc[1], cmp[1], sp * t.a.y);
+        tuned::two_sum(acc[2], cmp[2], sp * t.a.z);
+        tuned::two_sum(acc[3], cmp[3], sp * t.a.w);
+        tuned::two_sum(acc[4], cmp[4], sp * t.b.x);
+        tuned::two_sum(acc[5], cmp[5], sp * t.b.y);
+    }
+    __device__ __forceinline__ void pair(int pix, const float4& S, const F8& B, int bp, float c2,
+                                         float s2)
+    {
+        if (want_sky) sc.scatter(ga, gb, pix, B, c2, s2);
+        add(ga, gb, S, c2, s2, bp, 1.0f);
+    }
+    __device__ __forceinline__ void deferred(const tuned::Pend& p, int pix, const F8& B, int bp,
+                                            float c2, float s2, float&, float&)
+    {
+        if (want_sky) sc.scatter(p.ga, p.gb, pix, B, c2, s2);
+        add(p.ga, p.gb, fetch(pix), c2, s2, bp, 1.0f);
+    }
+    __device__ __forceinline__ void stencil(float wa, float wb, int pix, const float4& S,
+                                            const int px[4], const float w[4], float c2, float s2)
+    {
+        if (want_sky) {
+            F8 B;
+            B.a = make_float4(0.f, 0.f, 0.f, 0.f);
+            B.b = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (w[i] == 0.0f) continue;
+                const F8 v = tuned::load_beam(beam_base + px[i]);
+                B.a.x = fmaf(v.a.x, w[i], B.a.x); B.a.y = fmaf(v.a.y, w[i], B.a.y);
+                B.a.z = fmaf(v.a.z, w[i], B.a.z); B.a.w = fmaf(v.a.w, w[i], B.a.w);
+                B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);
+                B.b.z = fmaf(v.b.z, w[i], B.b.z); B.b.w = fmaf(v.b.w, w[i], B.b.w);
+            }
+            sc.scatter(wa, wb, pix, B, c2, s2);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (w[i] != 0.0f) add(wa, wb, S, c2, s2, px[i], w[i]);
+    }
+    __device__ __forceinline__ void pair_stencil(int pix, const float4& S, const int px[4],
+                                                 const float w[4], float c2, float s2)
+    {
+        stencil(ga, gb, pix, S, px, w, c2, s2);
+    }
+    __device__ __forceinline__ void deferred_stencil(const tuned::Pend& p, int pix, const int px[4],
+                                                     const float w[4], float c2, float s2)
+    {
+        stencil(p.ga, p.gb, pix, fetch(pix), px, w, c2, s2);
+    }
+    // the warp's six sums to row `warp` of ppart
+    __device__ __forceinline__ void finish(int lane, long long warp) const
+    {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            double v = (double)acc[k] + (double)cmp[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(tuned::kFull, v, o);
+            if (lane == 0) ppart[6 * warp + k] = v;
+        }
+    }
+};
+
+template <class A, class = void>
+struct HasFinish : std::false_type {};
+template <class A>
+struct HasFinish<A, std::void_t<decltype(&A::finish)>> : std::true_type {};
 
 // kBil: the transpose of the TUNED forward with the bilinear beam lookup.
 template <class Act, bool kBil>
@@ -237,6 +345,33 @@ __global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(Adj
     }
     tuned::flush<kBil>(hs, S, Q, lane, a.err, act);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
+    if constexpr (HasFinish<Act>::value) act.finish(lane, gw);
+}
+
+// Sum of the per-warp rows (6 doubles each) in warp order per thread, then a
+// fixed tree: one partial row in the layout of the Gaussian model's sums
+// (column 1: sum s g; columns 7..11: sum s dg/dt; the rest zero).
+__global__ void __launch_bounds__(256) fold_params_kernel(const double* ppart, int nwarps,
+                                                          double* row)
+{
+    __shared__ double sh[6][256];
+    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = threadIdx.x; w < nwarps; w += 256)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] += ppart[6 * w + k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < kParamCols) {
+        const int c = threadIdx.x;
+        row[c] = c == 1 ? sh[0][0] : (c >= 7 ? sh[c - 6][0] : 0.0);
+    }
 }
 
 // Fixed-order partial sums of |ga| + |gb| (one per block, then one block).
@@ -305,16 +440,21 @@ int resident_blocks(K kernel, int threads)
 }
 
 template <class Act>
-cudaError_t launch_act(const AdjArgs& a, const Act& act, int sm_count, cudaStream_t st)
+cudaError_t launch_act(const AdjArgs& a, const Act& act, int sm_count, cudaStream_t st,
+                       int* nwarps)
 {
     const long long need = (a.n + kAW - 1) / kAW;
+    long long blocks;
     if (a.interp == 1) {
-        long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, true>, kAW * 32);
-        adjoint_kernel<Act, true><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+        blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, true>, kAW * 32);
+        if (blocks > need) blocks = need;
+        adjoint_kernel<Act, true><<<(int)blocks, kAW * 32, 0, st>>>(a, act);
     } else {
-        long long blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, false>, kAW * 32);
-        adjoint_kernel<Act, false><<<(int)(blocks < need ? blocks : need), kAW * 32, 0, st>>>(a, act);
+        blocks = (long long)sm_count * resident_blocks(adjoint_kernel<Act, false>, kAW * 32);
+        if (blocks > need) blocks = need;
+        adjoint_kernel<Act, false><<<(int)blocks, kAW * 32, 0, st>>>(a, act);
     }
+    if (nwarps) *nwarps = (int)blocks * kAW;
     return cudaGetLastError();
 }
 
@@ -345,29 +485,63 @@ cudaError_t launch_fixed_to_float(const unsigned long long* in, void* out, int o
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st)
+int adjoint_max_warps(int sm_count) { return sm_count * 32 * kAW; }
+
+cudaError_t launch_fold_params(const double* ppart, int nwarps, double* row, cudaStream_t st)
 {
+    fold_params_kernel<<<1, 256, 0, st>>>(ppart, nwarps, row);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int* nwarps)
+{
+    if (nwarps) *nwarps = 0;
     if (a.n <= 0) return cudaSuccess;
+    if (a.ptab) {
+        if (a.fixed) {
+            ScatterParams<true> act{};
+            act.beam_base = a.beam32;
+            act.sky = a.sky32;
+            act.ptab = (const F8*)a.ptab;
+            act.ppart = a.ppart;
+            act.ci = a.ceps_i;
+            act.cq = a.ceps_q;
+            act.sc = Scatter<true>{0,       0,       nullptr,     a.gsky_fx,    nullptr,
+                                   nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v};
+            act.want_sky = a.gsky_fx != nullptr;
+            return launch_act(a, act, sm_count, st, nwarps);
+        }
+        ScatterParams<false> act{};
+        act.beam_base = a.beam32;
+        act.sky = a.sky32;
+        act.ptab = (const F8*)a.ptab;
+        act.ppart = a.ppart;
+        act.ci = a.ceps_i;
+        act.cq = a.ceps_q;
+        act.sc = Scatter<false>{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0, a.want_v};
+        act.want_sky = a.gsky32 != nullptr;
+        return launch_act(a, act, sm_count, st, nwarps);
+    }
     const bool beam = a.gbeam32 || a.gbeam_fx;
     if (a.fixed) {
         if (beam) {
             ScatterBeam<true> act{0,          0,         a.beam32,     a.sky32,
                                   nullptr,    a.gsky_fx, nullptr,      a.gbeam_fx,
                                   a.sky_scale, a.beam_scale, a.gsky_fx != nullptr, a.want_v};
-            return launch_act(a, act, sm_count, st);
+            return launch_act(a, act, sm_count, st, nwarps);
         }
         Scatter<true> act{0,       0,       nullptr,     a.gsky_fx,    nullptr,
                           nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v};
-        return launch_act(a, act, sm_count, st);
+        return launch_act(a, act, sm_count, st, nwarps);
     }
     if (beam) {
         ScatterBeam<false> act{0,         0,       a.beam32, a.sky32, a.gsky32,
                                nullptr,   a.gbeam32, nullptr, 0.0,   0.0,
                                a.gsky32 != nullptr, a.want_v};
-        return launch_act(a, act, sm_count, st);
+        return launch_act(a, act, sm_count, st, nwarps);
     }
     Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0, a.want_v};
-    return launch_act(a, act, sm_count, st);
+    return launch_act(a, act, sm_count, st, nwarps);
 }
 
 }  // namespace pisco

@@ -223,6 +223,46 @@ __global__ void __launch_bounds__(kBT) param_grad_kernel(Hpx h, long npix, Gauss
         for (int k = 0; k < kSums; ++k) part[kSums * blockIdx.x + k] = v[k];
 }
 
+// The model's weight and its derivatives at every beam pixel, for the fused
+// adjoint (adjoint.cu, ScatterParams): tab[p] = (g, dg/dF, dg/de, dg/dphi0 |
+// dg/ddx, dg/ddy, 0, 0) as floats, one 32-byte row per pixel; and the block
+// partials of sum g (column 0) and sum dg/dt (columns 2..6) in
+// param_grad_kernel's layout.  Columns 1 and 7..11 -- the sums weighted by
+// the beam-map gradient -- are left zero: the fused adjoint adds them as one
+// more row, and finish_kernel completes the gradient as for
+// param_grad_kernel.
+__global__ void __launch_bounds__(kBT) param_table_kernel(Hpx h, long npix, GaussDev gd,
+                                                          float4* __restrict__ tab,
+                                                          double* __restrict__ part)
+{
+    __shared__ double sh[kSums * 32];
+    double v[kSums];
+#pragma unroll
+    for (int k = 0; k < kSums; ++k) v[k] = 0.0;
+    const GaussModel& m = gd.m;
+    for (long p = blockIdx.x * (long)kBT + threadIdx.x; p < npix; p += (long)gridDim.x * kBT) {
+        double x, y;
+        const double g = gauss_at(h, gd, p, &x, &y);
+        const double dQ[5] = {x * x * m.aF + 2.0 * x * y * m.bF + y * y * m.cF,
+                              x * x * m.ae + 2.0 * x * y * m.be + y * y * m.ce,
+                              x * x * m.ap + 2.0 * x * y * m.bp + y * y * m.cp,
+                              -2.0 * (m.ca * x + m.cb * y), -2.0 * (m.cb * x + m.cc * y)};
+        double dg[5];
+        v[0] += g;
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            dg[t] = -g * dQ[t];
+            v[2 + t] += dg[t];
+        }
+        tab[2 * p] = make_float4((float)g, (float)dg[0], (float)dg[1], (float)dg[2]);
+        tab[2 * p + 1] = make_float4((float)dg[3], (float)dg[4], 0.f, 0.f);
+    }
+    block_sums<kSums>(v, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < kSums; ++k) part[kSums * blockIdx.x + k] = v[k];
+}
+
 // One block adds the first K columns of nblk partial rows, in block order per
 // thread then by the fixed tree, and finishes:
 //   kind 0 (PolBeam build): out[0..1] = sums x oc, + 1e-8 on the disabled side;
@@ -318,6 +358,29 @@ double ratio_sq(int nside_sky, int nside_beam)
 }
 
 }  // namespace
+
+namespace pisco {
+
+int gauss_table_rows(long npix) { return beam_grid(npix); }
+
+cudaError_t launch_gauss_param_table(int nside_beam, long npix, double fwhm_deg, double e,
+                                     double phi0_deg, double dx, double dy, float* tab,
+                                     double* part, cudaStream_t st)
+{
+    const GaussDev gd{gauss_model(fwhm_deg, e, phi0_deg), dx, dy};
+    param_table_kernel<<<beam_grid(npix), kBT, 0, st>>>(hpx_make(nside_beam), npix, gd,
+                                                         (float4*)tab, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gauss_param_finish(const double* part, int nrows, double oc, double* out,
+                                      cudaStream_t st)
+{
+    finish_kernel<kSums><<<1, kBT, 0, st>>>(nrows, part, 2, oc, 0, 0, out);
+    return cudaGetLastError();
+}
+
+}  // namespace pisco
 
 extern "C" {
 

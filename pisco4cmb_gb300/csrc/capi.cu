@@ -64,6 +64,7 @@ pisco_ctx::~pisco_ctx()
         if (s.beam) cudaFree(s.beam);
     for (void* p : {(void*)d_dets, (void*)d_items, (void*)d_queue, (void*)adj_sky32,
                     (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red,
+                    (void*)adj_ptab, (void*)adj_ppart,
                     (void*)rings, (void*)ord, (void*)ord_keys, (void*)ord_keys2,
                     (void*)ord_pos, ord_tmp, (void*)beam_scr})
         if (p) cudaFree(p);
@@ -335,8 +336,13 @@ pisco_status pisco_set_sky(pisco_ctx* c, int nside, const void* I, const void* Q
             }
         }
     }
+    // A failure of the first allocation leaves the previous sky in place (the
+    // maxMemUsage check) or no sky (cudaMalloc failed after the old buffer
+    // was freed); past it the device sky is being replaced, so the context
+    // reports NOT_READY until this call completes.
     st = c->ensure((void**)&c->sky32, &c->sky32_cap, sizeof(float4) * npix, "sky buffer");
     if (st != PISCO_OK) return st;
+    c->nside_sky = 0;
     CK(cudaMemcpyAsync(c->sky32, t32.data(), sizeof(float4) * npix, cudaMemcpyHostToDevice, c->stream),
        "sky H2D");
     c->sky64_valid = false;
@@ -367,6 +373,7 @@ pisco_status pisco_set_sky_device(pisco_ctx* c, int nside, const void* d_iquv, p
     const long long npix = 12LL * nside * nside;
     st = c->ensure((void**)&c->sky32, &c->sky32_cap, sizeof(float4) * npix, "sky buffer");
     if (st != PISCO_OK) return st;
+    c->nside_sky = 0;  // replaced from here on (see pisco_set_sky)
     if (dt == PISCO_FLOAT32) {
         CK(cudaMemcpyAsync(c->sky32, d_iquv, sizeof(float4) * npix, cudaMemcpyDeviceToDevice, s), "sky D2D");
         c->sky64_valid = false;
@@ -681,7 +688,8 @@ pisco_status pisco_tuned_calibrate(pisco_ctx* c, long begin, long n, double* wor
                                    long long* tuned_pairs)
 {
     if (!c || !worst) return PISCO_ERR_INVALID_ARGUMENT;
-    if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
+    if (!c->sky32 || !c->nside_sky || !c->beam32)
+        return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
     if (begin < 0 || n < 0 || begin + n > c->nsamples)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sample range outside the scan");
     if (!tuned_supported(c->nside_beam, (int)c->npix_beam, c->rho_max))

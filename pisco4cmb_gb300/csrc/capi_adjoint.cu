@@ -69,6 +69,23 @@ double fixed_scale(double bound)
     return std::ldexp(1.0, 62 - e);
 }
 
+// The fused Gaussian beam-parameter gradient of one adjoint call: the model
+// table and its partial rows (rows + 1 rows: the adjoint adds the last), the
+// per-warp partials, the result (5 device doubles) and the model's c.
+struct ParamPlan {
+    const float* tab;
+    double* part;
+    int rows;
+    double* ppart;
+    double* grad;
+    double oc;  // (nside_sky / nside_beam)^2
+    float ci, cq;
+};
+
+pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, const void* d_gb,
+                          pisco_dtype g_dtype, void* d_gsky, void* d_gbeam, pisco_dtype out_dtype,
+                          pisco_adjoint_mode mode, cudaStream_t s, const ParamPlan* pp);
+
 }  // namespace
 
 extern "C" {
@@ -110,11 +127,67 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
                                   pisco_dtype out_dtype, pisco_adjoint_mode mode, void* stream)
 {
     if (!c) return PISCO_ERR_INVALID_ARGUMENT;
-    if (!c->sky32 || !c->beam32) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
+    if (!d_gsky && !d_gbeam) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "no gradient output requested");
+    return adjoint_core(c, begin, n, d_ga, d_gb, g_dtype, d_gsky, d_gbeam, out_dtype, mode,
+                        stream ? (cudaStream_t)stream : c->stream, nullptr);
+}
+
+pisco_status pisco_adjoint_gaussian_device(pisco_ctx* c, long begin, long n, const void* d_ga,
+                                           const void* d_gb, pisco_dtype g_dtype, void* d_gsky,
+                                           pisco_dtype out_dtype, pisco_adjoint_mode mode,
+                                           double epsilon, int nside_sky, double fwhm_deg,
+                                           double ellipticity, double phi0_deg, double dx,
+                                           double dy, double* d_grad, void* stream)
+{
+    if (!c) return PISCO_ERR_INVALID_ARGUMENT;
+    if (!d_grad) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "grad must not be NULL");
+    if (nside_sky < 1 || nside_sky > 8192) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sky nside must be in [1, 8192]");
+    if (!(fwhm_deg > 0.0) || !std::isfinite(fwhm_deg) || !(std::fabs(ellipticity) < 1.0) ||
+        !std::isfinite(phi0_deg) || !std::isfinite(dx) || !std::isfinite(dy) || !std::isfinite(epsilon))
+        return fail(c, PISCO_ERR_INVALID_ARGUMENT,
+                    "model parameters: fwhm > 0, |ellipticity| < 1, the rest finite");
+    if (!c->beam32 || !c->nside_beam) return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
+    pisco_status st = c->activate();
+    if (st != PISCO_OK) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    const long npb = c->npix_beam;
+    const int rows = gauss_table_rows(npb);
+    const int max_warps = adjoint_max_warps(c->sm_count);
+    st = c->ensure((void**)&c->adj_ptab, &c->adj_ptab_cap, sizeof(float) * 8 * npb, "parameter table");
+    if (st != PISCO_OK) return st;
+    st = c->ensure((void**)&c->adj_ppart, &c->adj_ppart_cap,
+                   sizeof(double) * ((size_t)kParamCols * (rows + 1) + 6 * (size_t)max_warps),
+                   "parameter partials");
+    if (st != PISCO_OK) return st;
+    ParamPlan pp;
+    pp.tab = c->adj_ptab;
+    pp.part = c->adj_ppart;
+    pp.rows = rows;
+    pp.ppart = c->adj_ppart + (size_t)kParamCols * (rows + 1);
+    pp.grad = d_grad;
+    const double oc = (double)nside_sky / (double)c->nside_beam;
+    pp.oc = oc * oc;
+    pp.ci = (float)(1.0 + epsilon);
+    pp.cq = (float)(1.0 - epsilon);
+    CK(launch_gauss_param_table(c->nside_beam, npb, fwhm_deg, ellipticity, phi0_deg, dx, dy,
+                                c->adj_ptab, c->adj_ppart, s),
+       "parameter table");
+    return adjoint_core(c, begin, n, d_ga, d_gb, g_dtype, d_gsky, nullptr, out_dtype, mode, s, &pp);
+}
+
+}  // extern "C"
+
+namespace {
+
+pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, const void* d_gb,
+                          pisco_dtype g_dtype, void* d_gsky, void* d_gbeam, pisco_dtype out_dtype,
+                          pisco_adjoint_mode mode, cudaStream_t s, const ParamPlan* pp)
+{
+    if (!c->sky32 || !c->nside_sky || !c->beam32)
+        return fail(c, PISCO_ERR_NOT_READY, "sky and beam required");
     if (begin < 0 || n < 0 || begin + n > c->nsamples)
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "sample range outside the scan");
     if (n > 0 && (!d_ga || !d_gb)) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "TOD gradients are NULL");
-    if (!d_gsky && !d_gbeam) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "no gradient output requested");
     if ((g_dtype != PISCO_FLOAT32 && g_dtype != PISCO_FLOAT64) ||
         (out_dtype != PISCO_FLOAT32 && out_dtype != PISCO_FLOAT64))
         return fail(c, PISCO_ERR_INVALID_ARGUMENT, "bad dtype");
@@ -126,7 +199,6 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
         return fail(c, PISCO_ERR_UNSUPPORTED, "beam outside the adjoint's (TUNED) domain");
     pisco_status st = c->activate();
     if (st != PISCO_OK) return st;
-    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     const long long npix = 12LL * c->nside_sky * c->nside_sky;
     const long long nsky = 4 * npix, nbeam = 8LL * c->npix_beam;
     AdjArgs a{};
@@ -151,6 +223,13 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     if (st != PISCO_OK) return st;
     a.err = c->d_err;
     a.fallbacks = c->d_fallbacks;
+    if (pp) {
+        a.ptab = pp->tab;
+        a.ppart = pp->ppart;
+        a.ceps_i = pp->ci;
+        a.ceps_q = pp->cq;
+    }
+    int nwarps = 0;
     CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
     if (!deterministic) {
         a.fixed = 0;
@@ -176,7 +255,7 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
         }
         a.gsky32 = gs;
         a.gbeam32 = gbm;
-        if (n > 0) CK(launch_adjoint(a, c->sm_count, s), "adjoint launch");
+        if (n > 0) CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
         if (d_gsky && out_dtype == PISCO_FLOAT64) {
             widen_f32<<<1024, 256, 0, s>>>(gs, (double*)d_gsky, nsky);
@@ -223,8 +302,8 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
             CK(cudaMemsetAsync(c->adj_beam_fx, 0, 8 * nbeam, s), "zero beam accumulator");
             a.gbeam_fx = c->adj_beam_fx;
         }
-        if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0))
-            CK(launch_adjoint(a, c->sm_count, s), "adjoint launch");
+        if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0 || pp))
+            CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
         if (d_gsky)
             CK(launch_fixed_to_float(c->adj_sky_fx, d_gsky, out_dtype == PISCO_FLOAT64, nsky,
@@ -235,6 +314,12 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
                                      a.beam_scale > 0.0 ? 1.0 / a.beam_scale : 0.0, s),
                "beam gradient");
     }
+    if (pp) {
+        CK(launch_fold_params(pp->ppart, nwarps, pp->part + (size_t)kParamCols * pp->rows, s),
+           "parameter sums");
+        CK(launch_gauss_param_finish(pp->part, pp->rows + 1, pp->oc, pp->grad, s),
+           "parameter gradient");
+    }
     if (s != c->stream) {
         cudaEvent_t ev;
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
@@ -244,6 +329,10 @@ pisco_status pisco_adjoint_device(pisco_ctx* c, long begin, long n, const void* 
     }
     return PISCO_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 pisco_status pisco_adjoint(pisco_ctx* c, const void* g_a, const void* g_b, pisco_dtype g_dtype,
                            void* gI, void* gQ, void* gU, void* gV, pisco_dtype out_dtype,

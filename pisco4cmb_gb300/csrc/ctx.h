@@ -112,6 +112,11 @@ struct pisco_ctx {
     size_t adj_beam_fx_cap = 0;
     double* red = nullptr;
     size_t red_cap = 0;
+    // fused Gaussian beam-parameter gradient: model table, partial sums
+    float* adj_ptab = nullptr;
+    size_t adj_ptab_cap = 0;
+    double* adj_ppart = nullptr;
+    size_t adj_ppart_cap = 0;
 
     // device beam construction scratch (block partials, results, weights)
     double* beam_scr = nullptr;

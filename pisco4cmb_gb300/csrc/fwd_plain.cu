@@ -160,6 +160,43 @@ __device__ __forceinline__ void pair_accumulate(const FwdArgs& a, const Hpx& hs,
     }
 }
 
+// The disc of one sample: 32 rings per step, one per lane (HEALPix
+// query_disc's FP64 edge formula), flattened by a warp scan, the pairs
+// strided across lanes; f(pix) for every disc pixel.
+template <class F>
+__device__ __forceinline__ void walk_disc(const Hpx& hs, const DiscPlan& P, RingBatch& W, int lane,
+                                          unsigned int* err, F&& f)
+{
+    for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
+        const long long ring = r0 + lane;
+        RingSpan sp = {0, 0, 0, 0};
+        if (ring <= P.full_hi) sp = disc_ring(hs, P, ring);
+        const int cnt = (int)(sp.n1 + sp.n2);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        W.incl[lane] = incl;
+        W.cnt[lane] = cnt;
+        W.n1[lane] = (int)sp.n1;
+        W.s1[lane] = sp.start1;
+        W.s2[lane] = sp.start2;
+        __syncwarp();
+        for (int t = lane; t < total; t += 32) {
+            const long long pix = batch_pixel(W, t);
+            if (pix < 0 || pix >= hs.npix) {
+                record(err, kCheckSkyIndex);
+                continue;
+            }
+            f(pix);
+        }
+        __syncwarp();
+    }
+}
+
 template <bool F64>
 __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
 {
@@ -189,34 +226,9 @@ __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
         }
         const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, dec), ra, a.rho_max);
         double acc_a = 0.0, acc_b = 0.0;
-        for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
-            const long long ring = r0 + lane;
-            RingSpan sp = {0, 0, 0, 0};
-            if (ring <= P.full_hi) sp = disc_ring(hs, P, ring);
-            const int cnt = (int)(sp.n1 + sp.n2);
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int v = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const int total = __shfl_sync(kFull, incl, 31);
-            W.incl[lane] = incl;
-            W.cnt[lane] = cnt;
-            W.n1[lane] = (int)sp.n1;
-            W.s1[lane] = sp.start1;
-            W.s2[lane] = sp.start2;
-            __syncwarp();
-            for (int t = lane; t < total; t += 32) {
-                const long long pix = batch_pixel(W, t);
-                if (pix < 0 || pix >= hs.npix) {
-                    record(a.err, kCheckSkyIndex);
-                    continue;
-                }
-                pair_accumulate<F64>(a, hs, hb, pix, ra, dec, psi, acc_a, acc_b);
-            }
-            __syncwarp();
-        }
+        walk_disc(hs, P, W, lane, a.err, [&](long long pix) {
+            pair_accumulate<F64>(a, hs, hb, pix, ra, dec, psi, acc_a, acc_b);
+        });
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             acc_a += __shfl_xor_sync(kFull, acc_a, o);
@@ -231,6 +243,62 @@ __global__ void __launch_bounds__(kWarps * 32) plain_kernel(FwdArgs a)
                 if (a.out_b) ((float*)a.out_b)[j] = (float)acc_b;
             }
         }
+    }
+}
+
+// Record of the PLAIN form's decisions (pisco_debug_pairs): the same disc
+// walk and per-pair functions as plain_kernel, each pair written to its
+// sample's entries instead of accumulated.
+__global__ void __launch_bounds__(kWarps * 32) plain_dump_kernel(FwdArgs a, PairDump d)
+{
+    __shared__ RingBatch sh[kWarps];
+    const int lane = threadIdx.x & 31;
+    RingBatch& W = sh[threadIdx.x >> 5];
+    const Hpx hs = hpx_make(a.nside_sky);
+    const Hpx hb = hpx_make(a.nside_beam);
+    const long long gw = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const long long nw = (long long)gridDim.x * kWarps;
+    for (long long j = gw; j < a.n; j += nw) {
+        const long long s = a.begin + j;
+        const double ra = a.ra[s], dec = a.dec[s], psi = -a.pa[s];
+        if (!(isfinite(ra) && isfinite(dec) && isfinite(psi))) continue;
+        const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, dec), ra, a.rho_max);
+        walk_disc(hs, P, W, lane, a.err, [&](long long pix) {
+            const long long k = d.offset[j] + (long long)atomicAdd(&d.fill[j], 1u);
+            if (k >= d.offset[j + 1]) {
+                record(a.err, kCheckDump);
+                return;
+            }
+            double rho, sig, chi;
+            int flags = 0;
+            if (a.interp == 0) {
+                const long long bp = pair_beam_pixel(hs, hb, pix, ra, dec, psi, &rho, &sig, &chi);
+                d.beam_pix[k] = (int)bp;
+                if (bp < 0 || bp >= a.npix_beam) flags |= kPairOutside;
+            } else {
+                double th, ph;
+                pix2ang(hs, pix, &th, &ph);
+                rho_sigma_chi(ra, dec, psi, ph, PD_SUB(PD_DIV(kPi, 2.0), th), &rho, &sig, &chi);
+                int64_t px[4];
+                double w[4];
+                get_interpol(hb, rho, sig, px, w);
+                bool any = false;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    d.st_pix[4 * k + i] = (int)px[i];
+                    d.st_w[4 * k + i] = w[i];
+                    any |= px[i] >= 0 && px[i] < a.npix_beam;
+                }
+                d.beam_pix[k] = -1;
+                if (!any) flags |= kPairOutside;
+            }
+            d.sample[k] = (int)j;
+            d.sky_pix[k] = (int)pix;
+            d.chi[k] = chi;
+            d.c2[k] = (float)cos(2.0 * chi);
+            d.s2[k] = (float)sin(2.0 * chi);
+            d.flags[k] = flags;
+        });
     }
 }
 
@@ -318,6 +386,16 @@ cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaS
         long long need = (a.n + kWarps - 1) / kWarps;
         plain_kernel<false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dump_plain(const FwdArgs& a, const PairDump& d, int sm_count, cudaStream_t st)
+{
+    if (a.n <= 0) return cudaSuccess;
+    const int threads = kWarps * 32;
+    long long blocks = (long long)sm_count * resident_blocks(plain_dump_kernel, threads);
+    long long need = (a.n + kWarps - 1) / kWarps;
+    plain_dump_kernel<<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, d);
     return cudaGetLastError();
 }
 

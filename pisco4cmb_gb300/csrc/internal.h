@@ -54,6 +54,7 @@ enum DevCheck : unsigned int {
     kCheckFallbackOverflow = 3,
     kCheckQueue = 4,
     kCheckAdjointIndex = 5,
+    kCheckDump = 6,  // a pair record found its sample's entries full
 };
 
 struct FwdArgs {
@@ -143,9 +144,58 @@ struct AdjArgs {
     int interp;                    // 0 nearest, 1 bilinear beam lookup
     unsigned int* err;
     unsigned long long* fallbacks;
+    // fused Gaussian beam-parameter gradient (no beam-map gradient): the
+    // model table (npixB x 8 floats) or null, the per-warp partial sums
+    // (6 doubles per warp of the grid) and the model's (1 + eps, 1 - eps)
+    const float* ptab = nullptr;
+    double* ppart = nullptr;
+    float ceps_i = 1.0f, ceps_q = 1.0f;
 };
 
-cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st);
+// Per-pair record of a form's decisions (pisco_debug_pairs, debug.cu): the
+// pairs of the sample at position j fill entries [offset[j], offset[j+1]),
+// in no particular order (fill[j] counts the entries written so far).
+struct PairDump {
+    const long long* offset;  // n + 1 entries
+    unsigned int* fill;       // n entries, zero before the launch
+    int* sample;
+    int* sky_pix;
+    int* beam_pix;  // nearest lookup: the beam pixel; bilinear: -1
+    float* c2;      // cos 2chi, sin 2chi as the form multiplies by them
+    float* s2;
+    double* chi;    // PLAIN / FP64 forms: the FP64 chi; TUNED: NaN
+    int* flags;     // kPairRedone | kPairOutside
+    int* st_pix;    // bilinear stencil: 4 per entry
+    double* st_w;
+};
+constexpr int kPairRedone = 1;   // re-evaluated with the FP64 chain (TUNED)
+constexpr int kPairOutside = 2;  // beam pixel (or every stencil pixel) beyond the stored map
+// PLAIN-form record (fwd_plain.cu) and TUNED-form record (debug.cu) of
+// samples [a.begin, a.begin + a.n); a.order must be null.
+cudaError_t launch_dump_plain(const FwdArgs& a, const PairDump& d, int sm_count, cudaStream_t st);
+cudaError_t launch_dump_tuned(const FwdArgs& a, const PairDump& d, int sm_count, cudaStream_t st);
+
+// Fused beam-parameter gradient of the elliptical Gaussian pair model
+// (beam_model.h): a table of the model's weight and its five derivatives at
+// every beam pixel (npix x 8 floats) with the partial rows of its sums
+// (kParamCols doubles each, gauss_table_rows(npix) rows, beam_dev.cu); the
+// adjoint adds one row of beam-gradient-weighted sums (launch_fold_params);
+// launch_gauss_param_finish turns nrows rows into dL/d(F, e, phi0, dx, dy).
+constexpr int kParamCols = 12;
+int gauss_table_rows(long npix);
+cudaError_t launch_gauss_param_table(int nside_beam, long npix, double fwhm_deg, double e,
+                                     double phi0_deg, double dx, double dy, float* tab,
+                                     double* part, cudaStream_t st);
+cudaError_t launch_gauss_param_finish(const double* part, int nrows, double oc, double* out,
+                                      cudaStream_t st);
+// Sums the adjoint's per-warp partials (nwarps x 6) in warp order into one
+// partial row (columns 1 and 7..11; the rest zero).
+cudaError_t launch_fold_params(const double* ppart, int nwarps, double* row, cudaStream_t st);
+
+// Upper bound on the warps of an adjoint launch's grid.
+int adjoint_max_warps(int sm_count);
+// nwarps (optional): the warps of the launch's grid (the rows of ppart it writes).
+cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int* nwarps = nullptr);
 cudaError_t launch_abs_sum(const void* ga, const void* gb, int f64, long long n, double* part,
                            cudaStream_t st);
 cudaError_t launch_abs_max(const float* x, long long n, double* part, cudaStream_t st);

@@ -27,7 +27,10 @@
 // a device address; the device address is obtained once per device with
 // cudaGetSymbolAddress (with that device current) by the first call on that
 // device, and passed to the kernels.  That first call should therefore come
-// before any CUDA stream capture on the device.
+// before any CUDA stream capture on the device.  The address is cached for
+// the life of the process: a cudaDeviceReset of that device invalidates it,
+// so a process that resets a device must not call this entry point on it
+// afterwards.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -127,10 +130,15 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
         const pisco_noalloc_det& x = dets[d];
         if (x.nside_beam < 1 || x.nside_beam > 8192 || x.npix_beam < 1 ||
             x.npix_beam >= 12L * x.nside_beam * x.nside_beam || !x.beam_ab ||
-            ((uintptr_t)x.beam_ab & 15) || x.nsamples < 0 ||
+            ((uintptr_t)x.beam_ab & 31) || x.nsamples < 0 ||
             (x.nsamples > 0 && (!x.ra || !x.dec || !x.pa)))
             return reject(PISCO_ERR_INVALID_ARGUMENT,
-                          "noalloc: bad detector descriptor (beam size/alignment or NULL pointing)");
+                          "noalloc: bad detector descriptor (beam size, 32-byte alignment or NULL pointing)");
+        // same bound as the context-based batched forward; it also keeps the
+        // item count below from overflowing
+        if (x.nsamples > (1LL << 40))
+            return reject(PISCO_ERR_INVALID_ARGUMENT,
+                          "noalloc: more than 2^40 samples in one detector pair");
         const double rho = pisco_beam_rho_max(x.nside_beam, x.npix_beam);
         if (!tuned_supported(x.nside_beam, (int)x.npix_beam, rho))
             return reject(PISCO_ERR_UNSUPPORTED, "noalloc: a beam lies outside the TUNED form's domain");
@@ -156,8 +164,16 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
 
     // ---- once per device: the device address of the static scratch array
     int prev = -1;
-    if (cudaGetDevice(&prev) != cudaSuccess) return PISCO_ERR_CUDA;
-    if (cudaSetDevice(device) != cudaSuccess) return PISCO_ERR_CUDA;
+    cudaError_t es = cudaGetDevice(&prev);
+    if (es != cudaSuccess) {
+        cudaGetLastError();
+        return reject(PISCO_ERR_CUDA, cudaGetErrorString(es));
+    }
+    es = cudaSetDevice(device);
+    if (es != cudaSuccess) {
+        cudaGetLastError();
+        return reject(PISCO_ERR_CUDA, cudaGetErrorString(es));
+    }
     Scratch* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -174,9 +190,11 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
         scratch = g_scratch_ptr[device];
     }
     int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    es = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (es != cudaSuccess) {
+        cudaGetLastError();
         cudaSetDevice(prev);
-        return PISCO_ERR_CUDA;
+        return reject(PISCO_ERR_CUDA, cudaGetErrorString(es));
     }
     cudaStream_t st = (cudaStream_t)stream;
     noalloc_setup_kernel<<<1, 256, 0, st>>>(p, scratch);

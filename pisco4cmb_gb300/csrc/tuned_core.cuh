@@ -42,19 +42,27 @@
 //   kSums                     true: per-sample sums, TOD written per sample
 //   void reset(), total(a, b) main-pass sums (kSums)
 //   P fetch(int pix)          per-pixel data the action needs (Gather: the sky)
-//   void pair(int pix, P fetched, const F8& beam, float c2, float s2)
+//   void pair(int pix, P fetched, const F8& beam, int bp, float c2, float s2)
 //   void stash(Pend&)         per-sample data a queued pair needs later
-//   void deferred(const Pend&, int pix, const F8& beam, float c2, float s2,
+//   void deferred(const Pend&, int pix, const F8& beam, int bp, float c2, float s2,
 //                 float& ta, float& tb)      a re-evaluated pair
 //   kStencil                  true: with the bilinear lookup the action gets
 //                             the stencil instead of the interpolated value:
 //   void pair_stencil(int pix, P fetched, const int px[4], const float w[4], c2, s2)
 //   void deferred_stencil(const Pend&, int pix, const int px[4], const float w[4], c2, s2)
-// (c2, s2 = cos 2chi, sin 2chi; `beam` refers to the beam array element with
-// the nearest lookup, to the interpolated value with the bilinear one).
+// (c2, s2 = cos 2chi, sin 2chi; `beam` is the beam pixel's value, bp its
+// index, with the nearest lookup, and the interpolated value, bp = -1, with
+// the bilinear one).
+// Optional, detected at compile time (the forward and adjoint actions leave
+// them out, so they cost nothing there):
+//   void outside(int pix, int bp)                a disc pair whose beam pixel
+//   void outside_deferred(const Pend&, int pix, int bp)   lies beyond the
+//                             stored map (bp; -1: no bilinear stencil pixel in it)
 #pragma once
 
 #include <math_constants.h>
+
+#include <type_traits>
 
 #include "hpx.cuh"
 #include "internal.h"
@@ -74,6 +82,12 @@ namespace tuned {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kQCap = 64;
+
+// Does the action want to hear of disc pairs outside the stored beam map?
+template <class A, class = void>
+struct HasOutside : std::false_type {};
+template <class A>
+struct HasOutside<A, std::void_t<decltype(&A::outside)>> : std::true_type {};
 // Decisions whose FP32 value lies within kMarginRel * (value + 1) of an
 // integer are redone in FP64 (about 20 FP32 ulps).  The observed worst case
 // over a workload is measured by pisco_tuned_calibrate and must stay well
@@ -196,6 +210,24 @@ __device__ __forceinline__ bool near_int(float x, float m)
     return fabsf(x - rintf(x)) < m;
 }
 
+#ifndef PISCO_FAST_FLOOR
+#define PISCO_FAST_FLOOR 1
+#endif
+constexpr float kTwo23 = 8388608.0f;
+constexpr int kTwo23Bits = 0x4B000000;  // the bits of 2^23
+
+// floor(x) and its fractional part f = x - floor(x) for 0 <= x < 2^23 by
+// FP32 additions: x + 2^23 rounded down is 2^23 + floor(x) exactly (the
+// spacing of floats in [2^23, 2^24) is 1), and x - floor(x) is exact
+// (Sterbenz).  f < m or 1 - f < m is |x - rint(x)| < m (1 - f is exact for
+// f >= 1/2, and above 1/2 > m otherwise), so the decisions are near_int's.
+__device__ __forceinline__ int split_floor(float x, float& f)
+{
+    const float t = __fadd_rd(x, kTwo23);
+    f = x - (t - kTwo23);
+    return __float_as_int(t) - kTwo23Bits;
+}
+
 // 1/x by the MUFU reciprocal approximation (relative error below 2^-22);
 // used only for values, never for an index decision.
 __device__ __forceinline__ float rcp_approx(float x)
@@ -203,6 +235,34 @@ __device__ __forceinline__ float rcp_approx(float x)
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+}
+
+// One beam pixel, both detectors (32 bytes, one sector): a single 256-bit
+// load through the read-only path (PISCO_BEAM_LOAD 0: the compiler's own
+// loads, two 128-bit ones).
+#ifndef PISCO_BEAM_LOAD
+#define PISCO_BEAM_LOAD 1
+#endif
+__device__ __forceinline__ F8 load_beam(const F8* p)
+{
+#if PISCO_BEAM_LOAD == 0
+    return *p;
+#else
+    F8 r;
+#if PISCO_BEAM_LOAD == 2
+#define PISCO_LDB "ld.global.nc.L1::no_allocate.v8.f32"
+#elif PISCO_BEAM_LOAD == 3
+#define PISCO_LDB "ld.global.cg.v8.f32"
+#else
+#define PISCO_LDB "ld.global.nc.v8.f32"
+#endif
+    asm(PISCO_LDB " {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y),
+          "=f"(r.b.z), "=f"(r.b.w)
+        : "l"(p));
+#undef PISCO_LDB
+    return r;
+#endif
 }
 
 // The disc's pixel range(s) on one ring: FP32 edge angle, FP64 positions,
@@ -348,7 +408,7 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
     auto add = [&](int p, float w) {
         if (p >= B.npix) return;
         ws += w;
-        const F8 v = B.beam[p];
+        const F8 v = load_beam(B.beam + p);
         a.x = fmaf(v.a.x, w, a.x); a.y = fmaf(v.a.y, w, a.y);
         a.z = fmaf(v.a.z, w, a.z); a.w = fmaf(v.a.w, w, a.w);
         b.x = fmaf(v.b.x, w, b.x); b.y = fmaf(v.b.y, w, b.y);
@@ -462,14 +522,21 @@ __device__ __forceinline__ void drain(const Hpx& hs, int m, WarpSmem& S, Queue& 
             float w[4];
             if (stencil_f64(P.hb, P.npix_beam, rho, sig, px, w))
                 act.deferred_stencil(P, pix, px, w, (float)cos(2.0 * chi), (float)sin(2.0 * chi));
+            else if constexpr (HasOutside<Action>::value)
+                act.outside_deferred(P, pix, -1);
         } else if constexpr (kBil) {
             F8 Bv;
             if (bilinear_f64(P.hb, P.npix_beam, rho, sig, P.beam, Bv))
-                act.deferred(P, pix, Bv, (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+                act.deferred(P, pix, Bv, -1, (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+            else if constexpr (HasOutside<Action>::value)
+                act.outside_deferred(P, pix, -1);
         } else if (bp < 0) {
             record(err, kCheckBeamIndex);
         } else if (bp < P.npix_beam) {
-            act.deferred(P, pix, P.beam[bp], (float)cos(2.0 * chi), (float)sin(2.0 * chi), ta, tb);
+            act.deferred(P, pix, load_beam(P.beam + bp), (int)bp, (float)cos(2.0 * chi),
+                         (float)sin(2.0 * chi), ta, tb);
+        } else if constexpr (HasOutside<Action>::value) {
+            act.outside_deferred(P, pix, (int)bp);
         }
     }
     if (Action::kSums) {
@@ -765,6 +832,8 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                             float c2, s2;
                             phasor(c2, s2);
                             act.pair_stencil(pix, act.fetch(pix), px, w, c2, s2);
+                        } else if constexpr (HasOutside<Action>::value) {
+                            if (!fb) act.outside(pix, -1);
                         }
                     } else if constexpr (kBil) {
                         fb = q < kTinyQ;
@@ -772,11 +841,28 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                         if (!fb && bilinear_f32(B, qd, tp, r, Bv)) {
                             float c2, s2;
                             phasor(c2, s2);
-                            act.pair(pix, act.fetch(pix), Bv, c2, s2);
+                            act.pair(pix, act.fetch(pix), Bv, -1, c2, s2);
+                        } else if constexpr (HasOutside<Action>::value) {
+                            if (!fb) act.outside(pix, -1);
                         }
                     } else {
                         const float av = tp * r;
                         const float bv = (1.0f - tp) * r;
+#if PISCO_FAST_FLOOR
+                        // floors and fractional parts by FP32 additions (no
+                        // conversion instructions), the same values as the
+                        // conversions: see split_floor
+                        float fa, fbv, fc;
+                        const int jp = split_floor(av, fa), jm = split_floor(bv, fbv);
+                        const int ir = jp + jm + 1;
+                        const float irf = __int_as_float(ir + kTwo23Bits) - kTwo23;
+                        const float cv = tp * irf;
+                        const int ipr = split_floor(cv, fc);
+                        const float m = kMarginRel * (r + 1.0f);
+                        const float mc = kMarginRel * (irf + 1.0f);
+                        fb = q < kTinyQ || fa < m || 1.0f - fa < m || fbv < m ||
+                             1.0f - fbv < m || fc < mc || 1.0f - fc < mc;
+#else
                         const int jp = (int)av, jm = (int)bv;
                         const int ir = jp + jm + 1;
                         const float cv = tp * (float)ir;
@@ -784,6 +870,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                         const float m = kMarginRel * (r + 1.0f);
                         fb = q < kTinyQ || near_int(av, m) || near_int(bv, m) ||
                              near_int(cv, kMarginRel * ((float)ir + 1.0f));
+#endif
                         if (kCalib && !fb) {
                             double rho, sig, chi;
                             (void)pair_beam_pixel(hs, hb, pix, F.ra, F.dec, F.psi, &rho, &sig, &chi);
@@ -800,7 +887,9 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                             if (bp >= 0 && bp < B.npix) {
                                 float c2, s2;
                                 phasor(c2, s2);
-                                act.pair(pix, act.fetch(pix), B.beam[bp], c2, s2);
+                                act.pair(pix, act.fetch(pix), load_beam(B.beam + bp), bp, c2, s2);
+                            } else if constexpr (HasOutside<Action>::value) {
+                                act.outside(pix, bp);
                             }
                         }
                     }
@@ -857,7 +946,7 @@ struct Gather {
         tb = S.x * B.b.x + S.y * (-B.b.y * c2 + B.b.z * s2) + S.z * (-B.b.z * c2 - B.b.y * s2) +
              S.w * B.b.w;
     }
-    __device__ __forceinline__ void pair(int, const float4& S, const F8& B, float c2, float s2)
+    __device__ __forceinline__ void pair(int, const float4& S, const F8& B, int, float c2, float s2)
     {
         float ta, tb;
         contrib(S, B, c2, s2, ta, tb);
@@ -865,7 +954,7 @@ struct Gather {
         two_sum(sb, cb, tb);
     }
     __device__ __forceinline__ void stash(Pend&) const {}
-    __device__ __forceinline__ void deferred(const Pend&, int pix, const F8& B, float c2, float s2,
+    __device__ __forceinline__ void deferred(const Pend&, int pix, const F8& B, int, float c2, float s2,
                                             float& ta, float& tb) const
     {
         contrib(fetch(pix), B, c2, s2, ta, tb);

@@ -9,10 +9,12 @@ fixed array compiled into the library.
 This test calls that entry point through the C ABI twice in a row, with
 two different detector sets (different beams, sizes and chunking), and
 compares each result with the context-based batched forward
-(pisco_forward_batched) on the same inputs, at the TUNED tolerance used by
-the other tests (1e-6 of the TOD rms; the two run the same kernel, so the
-results are expected to be identical).  It also checks that sizes beyond
-the fixed array are refused with a clear message and no GPU work.
+(pisco_forward_batched) on the same inputs.  The two run the same kernel on
+the same inputs and each sample's TOD does not depend on how the samples
+are cut into work items, so the results must be identical bit for bit.  A
+third call runs on a caller-owned stream with one detector's b output left
+NULL.  It also checks that sizes beyond the fixed array are refused with a
+clear message and no GPU work.
 
 The file is named to be collected last, so a run that stops at the first
 failure has already run every other test.
@@ -21,8 +23,6 @@ import ctypes
 
 import numpy as np
 import pytest
-
-from conftest import rel_max
 
 pytestmark = pytest.mark.gpu
 
@@ -53,7 +53,7 @@ def _detector_set(seed, ndet, nss=64, nsb=256):
     return sky, nss, dets
 
 
-def _noalloc(sky, nss, dets, chunk):
+def _noalloc(sky, nss, dets, chunk, stream=None, no_b=()):
     import torch
 
     from pisco4cmb_gb300 import _lib
@@ -67,11 +67,13 @@ def _noalloc(sky, nss, dets, chunk):
         outs.append((ta, tb))
         arr[i] = _lib.NoallocDet(d["beam"].nside, d["beam"].nPixels, d["ab"].data_ptr(), d["n"],
                                  d["ra"].data_ptr(), d["dec"].data_ptr(), d["pa"].data_ptr(),
-                                 ta.data_ptr(), tb.data_ptr())
+                                 ta.data_ptr(), None if i in no_b else tb.data_ptr())
     torch.cuda.synchronize()
+    handle = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
     st = L.pisco_forward_batched_noalloc(0, nss, ctypes.c_void_p(sky.data_ptr()), arr, len(dets),
-                                         chunk, None)
+                                         chunk, handle)
     assert st == 0, L.pisco_last_error(None)
+    torch.cuda.synchronize()
     return [(a.cpu().numpy(), b.cpu().numpy()) for a, b in outs]
 
 
@@ -105,7 +107,22 @@ def test_noalloc_matches_batched_forward_twice(gpu):
         want = _existing(sky, nss, dets)
         for (ga, gb), (wa, wb) in zip(got, want):
             assert np.all(np.isfinite(ga)) and np.all(np.isfinite(gb))
-            assert rel_max(ga, wa) <= 1e-6 and rel_max(gb, wb) <= 1e-6
+            assert np.array_equal(ga, wa) and np.array_equal(gb, wb)
+
+
+def test_noalloc_on_caller_stream_with_a_null_output(gpu):
+    import torch
+
+    sky, nss, dets = _detector_set(44, 4)
+    want = _existing(sky, nss, dets)
+    stream = torch.cuda.Stream()
+    got = _noalloc(sky, nss, dets, 128, stream=stream, no_b=(2,))
+    for i, ((ga, gb), (wa, wb)) in enumerate(zip(got, want)):
+        assert np.array_equal(ga, wa)
+        if i == 2:
+            assert np.all(np.isnan(gb))  # NULL output: the buffer is never written
+        else:
+            assert np.array_equal(gb, wb)
 
 
 def test_noalloc_rejects_sizes_beyond_its_array(gpu):
@@ -132,3 +149,11 @@ def test_noalloc_rejects_sizes_beyond_its_array(gpu):
     st = L.pisco_forward_batched_noalloc(0, nss, ctypes.c_void_p(sky.data_ptr()), one, 1, 1, None)
     assert st == _lib.PISCO_ERR_INVALID_ARGUMENT
     assert b"PISCO_NOALLOC_MAX_ITEMS" in L.pisco_last_error(None)
+    huge_row = _lib.NoallocDet(d["beam"].nside, d["beam"].nPixels, d["ab"].data_ptr(),
+                               (1 << 62), d["ra"].data_ptr(), d["dec"].data_ptr(),
+                               d["pa"].data_ptr(), None, None)
+    one = (_lib.NoallocDet * 1)(huge_row)
+    st = L.pisco_forward_batched_noalloc(0, nss, ctypes.c_void_p(sky.data_ptr()), one, 1, 1 << 30,
+                                         None)
+    assert st == _lib.PISCO_ERR_INVALID_ARGUMENT
+    assert b"2^40" in L.pisco_last_error(None)
