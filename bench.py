@@ -598,17 +598,19 @@ def run_c4_batched(args):
     total = sum(p["nsamples"] for p in dets)
     cache = os.path.join(os.environ.get("PISCO_TUNE_CACHE", "/tmp"), "pisco_autotune.json")
     chunk, tune_ms = conv.autotune_batched(descs, cache_path=cache)
+    _, warps = conv.batched_config()
     cs = _study_stream()
     for _ in range(2):
         conv.forward_batched(descs, stream=cs)
     conv.sync()
     e0, e1 = _events()
-    e0.record()
-    for _ in range(args.steps):
-        conv.forward_batched(descs, stream=cs)
-    e1.record()
-    conv.sync()
-    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            conv.forward_batched(descs, stream=cs)
+        e1.record()
+        conv.sync()
+        torch.cuda.synchronize()
     t_batched = e0.elapsed_time(e1) / 1e3 / args.steps
     batched_out = [[o.cpu().numpy() for o in k[1]] for k in keep]
     # sequential single-detector launches (TUNED and PLAIN), one context each pair
@@ -638,12 +640,64 @@ def run_c4_batched(args):
         seq[form] = {"samples_per_s": nseq / tt, "samples": nseq, "bit_identical_to_batched":
                      same if form == "tuned" else None}
         c.close()
+    # many short scans: 512 pairs of 2,000 samples (the 48 beams in turn),
+    # where one launch per pair leaves most of the GPU idle
+    m_small, n_small = 2000, 512
+    srows, skeep, sscans = [], [], []
+    for k in range(n_small):
+        d = k % len(dets)
+        ra, dec, pa = scans[d]
+        off = (k * 7919) % max(1, dets[d]["nsamples"] - m_small)
+        sl = slice(off, off + m_small)
+        t = [torch.tensor(np.ascontiguousarray(x[sl]), device="cuda") for x in (ra, dec, pa)]
+        o = [torch.empty(m_small, device="cuda") for _ in range(2)]
+        skeep.append((t, o))
+        sscans.append(d)
+        srows.append((d, m_small, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(),
+                      o[0].data_ptr(), o[1].data_ptr()))
+    sdescs = conv.det_descs(srows)
+    s_chunk, _ = conv.autotune_batched(sdescs, cache_path=cache)
+    _, s_warps = conv.batched_config()
+    conv.forward_batched(sdescs, stream=cs)
+    conv.sync()
+    e0.record()
+    for _ in range(args.steps):
+        conv.forward_batched(sdescs, stream=cs)
+    e1.record()
+    conv.sync()
+    torch.cuda.synchronize()
+    t_small = e0.elapsed_time(e1) / 1e3 / args.steps
+    c = GPUConvolver(form="tuned")
+    c.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    tt = 0.0
+    same = True
+    for k, d in enumerate(sscans):
+        c.update_beam(beams[d])
+        t, _ = skeep[k]
+        c.set_scan_device(m_small, *[x.data_ptr() for x in t])
+        oa = torch.empty(m_small, device="cuda")
+        ob = torch.empty(m_small, device="cuda")
+        e0.record()
+        c.forward_device(oa.data_ptr(), ob.data_ptr(), stream=cs)
+        e1.record()
+        torch.cuda.synchronize()
+        tt += e0.elapsed_time(e1) / 1e3
+        same &= bool(torch.equal(oa, skeep[k][1][0]))
+    c.close()
+    small = {"pairs": n_small, "samples_per_pair": m_small, "autotuned_chunk": s_chunk,
+             "autotuned_warps_per_block": s_warps,
+             "batched_samples_per_s": n_small * m_small / t_small,
+             "sequential_tuned_samples_per_s": n_small * m_small / tt,
+             "batched_over_sequential_tuned": tt / t_small,
+             "bit_identical_to_batched": same}
     line = {"workload": "c4_batched_48pairs_nside512", "ndet": len(dets), "total_samples": total,
-            "autotuned_chunk": chunk, "autotune_best_ms": tune_ms,
+            "autotuned_chunk": chunk, "autotuned_warps_per_block": warps,
+            "autotune_best_ms": tune_ms,
             "batched_graph_samples_per_s": total / t_batched, "batched_ms": t_batched * 1e3,
             "sequential_tuned": seq["tuned"], "sequential_plain": seq["plain"],
             "batched_over_sequential_tuned": (total / t_batched) / seq["tuned"]["samples_per_s"],
-            "batched_over_sequential_plain": (total / t_batched) / seq["plain"]["samples_per_s"]}
+            "batched_over_sequential_plain": (total / t_batched) / seq["plain"]["samples_per_s"],
+            "many_short_scans": small, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0
 

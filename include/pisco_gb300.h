@@ -239,14 +239,22 @@ pisco_status pisco_set_beam_slot(pisco_ctx* ctx, int slot, int nside, long npix,
  * (PISCO_ERR_UNSUPPORTED otherwise). */
 pisco_status pisco_forward_batched(pisco_ctx* ctx, const pisco_det_desc* dets, int ndet,
                                    pisco_dtype out_dtype, int chunk, void* stream);
-/* Autotuner (no reference counterpart): times the batched launch for chunk
- * sizes 32..8192 on these descriptors, keeps the fastest in the context and,
- * if cache_path is not NULL, in a JSON object keyed by device, sky nside,
- * beam set and form (read first: a cached key is reused without timing).
- * Returns the chosen chunk and its time in ms. */
+/* Autotuner (no reference counterpart): times the batched launch on these
+ * descriptors for each tile -- 4, 8 or 16 warps per block, every shape at 16
+ * warps per SM -- and chunk sizes 32..8192, keeps the fastest pair in the
+ * context and, if cache_path is not NULL, in a JSON object keyed by device,
+ * sky nside, beam set, output type and beam lookup (read first: a cached key
+ * is reused without timing).  Returns the chosen chunk and its time in ms;
+ * pisco_batched_config reports the chosen tile. */
 pisco_status pisco_autotune_batched(pisco_ctx* ctx, const pisco_det_desc* dets, int ndet,
                                     pisco_dtype out_dtype, const char* cache_path,
                                     int* chunk_out, double* ms_out);
+/* The chunk (0 passed to pisco_forward_batched means this one) and warps per
+ * block the batched launch uses now (either pointer may be NULL). */
+pisco_status pisco_batched_config(pisco_ctx* ctx, int* chunk, int* warps_per_block);
+/* Sets them without timing (chunk 0 keeps the current chunk; warps per block
+ * 4, 8 or 16). */
+pisco_status pisco_set_batched_config(pisco_ctx* ctx, int chunk, int warps_per_block);
 
 /* ---- allocation-free batched forward (no counterpart in the reference) --
  * For callers that may not allocate device memory (real-time loops, host
@@ -429,6 +437,35 @@ pisco_status pisco_map_get_normal(pisco_map* map, double* ata, double* atd);
  * [2][2], then AtD[0..2], each as one npix-long plane). */
 pisco_status pisco_map_device_arrays(pisco_map* map, const float** d_iqu, const int** d_hits,
                                      const double** d_normal);
+
+/* ---- detector pointing from the array centre (BPoint::focal_plane_to_sky,
+ *      src/Bpoint/bpoint.cpp:553-674, src/Bpoint/BPoint.h:99-103) ----------
+ * The geometry-only step of BPoint (its ephemeris part needs SOFA and JPL
+ * tables, which the reference tree does not hold): per detector, receiver-
+ * frame offsets det_dx (positive right) and det_dy (positive up) and the
+ * polarization angle ccw from the receiver y axis; per sample, the array
+ * centre (x_ac, y_ac) and rot_ac, the angle of the receiver's up axis from
+ * the zenith (flag 0, Az/El), the celestial pole (flag 1, Ra/Dec) or the
+ * source (flag 2, source-relative).  Outputs ndets x nsamples, indexed
+ * [det * nsamples + s]: longitude (Ra/Az; flag 2: bearing), latitude and the
+ * detector's polarization direction (position angle + polarization angle).
+ * Radians; FP64 on the GPU.  Host arrays, synchronous, current device.
+ * A beam model's centre offset (dx, dy) (pisco_beam_gaussian_device) is, to
+ * first order, the focal-plane offset (det_dx, det_dy) = (-dy, -dx) of a
+ * detector whose scan position angle is rot_ac. */
+pisco_status pisco_focal_plane_to_sky(int ndets, const double* det_dx, const double* det_dy,
+                                      const double* det_pol_angle, long nsamples,
+                                      const double* x_ac, const double* y_ac,
+                                      const double* rot_ac, int flag, double* x_det,
+                                      double* y_det, double* rot_det);
+/* Same with device arrays, on `stream` (NULL: the legacy default stream);
+ * asynchronous. */
+pisco_status pisco_focal_plane_to_sky_device(int ndets, const double* d_det_dx,
+                                             const double* d_det_dy, const double* d_det_pol,
+                                             long nsamples, const double* d_x_ac,
+                                             const double* d_y_ac, const double* d_rot_ac, int flag,
+                                             double* d_x_det, double* d_y_det, double* d_rot_det,
+                                             void* stream);
 
 /* ---- host HEALPix / PolBeam helpers (for the C++ PolBeam wrapper) ------ */
 /* Healpix_Base::pix2ang / ang2pix, RING (used by polbeam.cpp:130,441). */

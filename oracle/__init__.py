@@ -185,6 +185,19 @@ def query_disc(nside: int, theta: float, phi: float, radius: float) -> np.ndarra
     return out
 
 
+def focal_plane_to_sky(det_dx, det_dy, det_pol, x_ac, y_ac, rot_ac, flag: int = 1):
+    """BPoint::focal_plane_to_sky restated (bpoint.cpp:553-674): outputs
+    (x_det, y_det, rot_det), each ndets x nsamples."""
+    dx, dy, dp = (_c(np.atleast_1d(x), np.float64) for x in (det_dx, det_dy, det_pol))
+    xa, ya, ra_ = (_c(x, np.float64) for x in (x_ac, y_ac, rot_ac))
+    nd, ns = dx.size, xa.size
+    out = [np.empty((nd, ns), np.float64) for _ in range(3)]
+    lib().orc_focal_plane_to_sky(ctypes.c_int(nd), _ptr(dx), _ptr(dy), _ptr(dp), _i64(ns),
+                                 _ptr(xa), _ptr(ya), _ptr(ra_), ctypes.c_int(flag),
+                                 *[_ptr(o) for o in out])
+    return tuple(out)
+
+
 def match_pairs(ra, dec, pa, skypix, nside_sky: int, nside_beam: int):
     ra, dec, pa = (_c(x, np.float64) for x in (ra, dec, pa))
     sp = _c(skypix, np.int64)

@@ -892,3 +892,47 @@ void orc_map_solve(int64_t npix, const double* ata, const double* atd, float* I,
         hits[p] = h;
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Focal plane to sky (src/Bpoint/bpoint.cpp:553-674)                   */
+/* ------------------------------------------------------------------ */
+/* Restates BPoint::focal_plane_to_sky, the spherical triangle between the
+ * array centre, the detector and the pole (zenith, celestial pole or
+ * source): the detector sits at angular distance r = acos(cos dx cos dy)
+ * from the array centre, in the receiver-frame direction a = atan2(sin dy,
+ * sin dx cos dy) from the receiver x axis; g = pi/2 - a - rot is the angle
+ * detector -> array centre -> pole.  Outputs [det * nsamples + s]. */
+void orc_focal_plane_to_sky(int ndets, const double* det_dx, const double* det_dy,
+                            const double* det_pol, int64_t nsamples, const double* x_ac,
+                            const double* y_ac, const double* rot_ac, int flag,
+                            double* x_det, double* y_det, double* rot_det)
+{
+    for (int d = 0; d < ndets; ++d) {
+        const double cx = cos(det_dx[d]), sx = sin(det_dx[d]);
+        const double cy_r = cos(det_dy[d]), sy_r = sin(det_dy[d]);
+        const double cr = cx * cy_r;                      /* cos r */
+        const double sr = sqrt((1.0 - cr) * (1.0 + cr));  /* sin r */
+        const double a = atan2(sy_r, sx * cy_r);
+        for (int64_t s = 0; s < nsamples; ++s) {
+            const int64_t k = (int64_t)d * nsamples + s;
+            const double g = O_HALFPI - a - rot_ac[s];
+            const double cg = cos(g), sg = sin(g);
+            const double sl = sin(y_ac[s]), cl = cos(y_ac[s]);
+            const double se = sin(rot_ac[s]), ce = cos(rot_ac[s]);
+            /* latitude of the detector: law of cosines in the triangle */
+            y_det[k] = asin(cr * sl + sr * cl * cg);
+            /* position angle at the detector of the receiver-frame pole */
+            const double num = cl * se * cx - sl * sx;
+            const double den = cl * ce * cy_r - (sl * cx + cl * se * sx) * sy_r;
+            const double pa = atan2(num, den);
+            rot_det[k] = pa + det_pol[d];
+            if (flag == 2) {
+                x_det[k] = -pa;
+            } else {
+                /* longitude step from the array centre to the detector */
+                const double dl = atan2(sr * sg, cr * cl - sr * sl * cg);
+                x_det[k] = flag == 0 ? x_ac[s] + dl : x_ac[s] - dl;
+            }
+        }
+    }
+}

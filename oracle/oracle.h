@@ -23,6 +23,9 @@
  *     convolver.cpp:162-185, with the weight renormalisation it intends).
  *   - the PolBeam builders restated from src/Polbeam/polbeam.cpp:108-133,
  *     212-279, 281-383, 385-467.
+ *   - BPoint::focal_plane_to_sky restated from src/Bpoint/bpoint.cpp:553-674
+ *     (spherical trigonometry only; the ephemeris part of BPoint needs SOFA
+ *     and JPL data, absent from the reference tree).
  *
  * Parity pins: see tests/test_oracle_*.py.  The HEALPix part is pinned
  * against the reference's own device port (cudaHealpix.cu compiled for the
@@ -168,6 +171,16 @@ int orc_dgesv3(double* a, int* ipiv, double* b);
  * keeps AtD as I, Q, U and sets hits to 0.  hits < 3: I = Q = U = 0. */
 void orc_map_solve(int64_t npix, const double* ata, const double* atd, float* I, float* Q,
                    float* U, int* hits);
+
+/* ---------------- focal plane to sky (src/Bpoint/bpoint.cpp:553-674) ---- */
+/* BPoint::focal_plane_to_sky: detector pointing from the array centre's
+ * (x_ac, y_ac, rot_ac) and the receiver-frame offsets (det_dx right,
+ * det_dy up) and polarization angles; flag 0 Az/El, 1 Ra/Dec, 2
+ * source-relative.  Outputs ndets x nsamples, [det * nsamples + s]. */
+void orc_focal_plane_to_sky(int ndets, const double* det_dx, const double* det_dy,
+                            const double* det_pol, int64_t nsamples, const double* x_ac,
+                            const double* y_ac, const double* rot_ac, int flag,
+                            double* x_det, double* y_det, double* rot_det);
 
 #ifdef __cplusplus
 }

@@ -9,8 +9,8 @@ package is its host-side mirror of the reference API.
 """
 from .api import (Convolver, GPUConvolver, PiscoError, PiscoInvalidArgument, PolBeam,  # noqa: F401
                   RunConfig, Scan, Sky, SkyMap, ang2pix, beam_npix_for_radius,
-                  gaussian_beam_param_grad, pix2ang)
+                  focal_plane_to_sky, gaussian_beam_param_grad, pix2ang)
 
 __all__ = ["Convolver", "GPUConvolver", "PiscoError", "PiscoInvalidArgument", "PolBeam",
            "RunConfig", "Scan", "Sky", "SkyMap", "ang2pix", "beam_npix_for_radius",
-           "gaussian_beam_param_grad", "pix2ang"]
+           "focal_plane_to_sky", "gaussian_beam_param_grad", "pix2ang"]

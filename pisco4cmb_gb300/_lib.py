@@ -133,12 +133,16 @@ SIGNATURES = [
     ("pisco_forward_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, _I, _P]),
     ("pisco_autotune_batched", _S, [_P, ctypes.POINTER(DetDesc), _I, _I, ctypes.c_char_p,
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    ("pisco_batched_config", _S, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    ("pisco_set_batched_config", _S, [_P, _I, _I]),
     ("pisco_forward_batched_noalloc", _S, [_I, _I, _P, ctypes.POINTER(NoallocDet), _I, _I, _P]),
     ("pisco_set_beam_device", _S, [_P, _I, _L, _P, _I, _P]),
     ("pisco_adjoint_device", _S, [_P, _L, _L, _P, _P, _I, _P, _P, _I, _I, _P]),
     ("pisco_adjoint", _S, [_P, _P, _P, _I, _P, _P, _P, _P, _I, _I]),
     ("pisco_adjoint_gaussian_device", _S, [_P, _L, _L, _P, _P, _I, _P, _I, _I, _D, _I, _D, _D,
                                            _D, _D, _D, _P, _P]),
+    ("pisco_focal_plane_to_sky", _S, [_I, _P, _P, _P, _L, _P, _P, _P, _I, _P, _P, _P]),
+    ("pisco_focal_plane_to_sky_device", _S, [_I, _P, _P, _P, _L, _P, _P, _P, _I, _P, _P, _P, _P]),
     ("pisco_hpx_pix2ang", _S, [_I, _L, _P, _P, _P]),
     ("pisco_hpx_ang2pix", _S, [_I, _L, _P, _P, _P]),
     ("pisco_beam_npix_for_radius", _L, [_I, _D]),

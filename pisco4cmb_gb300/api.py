@@ -30,7 +30,7 @@ from ._lib import (FLOAT32, FLOAT64, FORMS, PiscoError, PiscoInvalidArgument, Ru
 
 __all__ = ["Scan", "Sky", "PolBeam", "Convolver", "GPUConvolver", "SkyMap", "RunConfig",
            "PiscoError", "PiscoInvalidArgument", "beam_npix_for_radius", "pix2ang", "ang2pix",
-           "gaussian_beam_param_grad"]
+           "gaussian_beam_param_grad", "focal_plane_to_sky"]
 
 
 def _ptr(a: np.ndarray):
@@ -62,6 +62,25 @@ def ang2pix(nside: int, theta, phi):
     out = np.empty(th.shape, np.int64)
     check(L.pisco_hpx_ang2pix(nside, th.size, _ptr(th), _ptr(ph), _ptr(out)), None, "ang2pix")
     return out
+
+
+def focal_plane_to_sky(det_dx, det_dy, det_pol_angle, x_ac, y_ac, rot_ac, flag: int = 1):
+    """BPoint::focal_plane_to_sky (src/Bpoint/bpoint.cpp:553-674) on the GPU:
+    detector pointing from the array centre's.  det_*: per detector (receiver
+    offsets right / up and polarization angle, radians); x_ac, y_ac, rot_ac:
+    per sample; flag 0 Az/El, 1 Ra/Dec, 2 source-relative.  Returns
+    (x_det, y_det, rot_det), each ndets x nsamples."""
+    L = load()
+    dx, dy, dp = (np.ascontiguousarray(np.atleast_1d(v), dtype=np.float64)
+                  for v in (det_dx, det_dy, det_pol_angle))
+    xa, ya, ra = (np.ascontiguousarray(v, dtype=np.float64) for v in (x_ac, y_ac, rot_ac))
+    if not (dx.size == dy.size == dp.size and xa.size == ya.size == ra.size):
+        raise PiscoInvalidArgument(1, "detector arrays and sample arrays must match in length")
+    out = [np.empty((dx.size, xa.size), np.float64) for _ in range(3)]
+    check(L.pisco_focal_plane_to_sky(dx.size, _ptr(dx), _ptr(dy), _ptr(dp), xa.size, _ptr(xa),
+                                     _ptr(ya), _ptr(ra), int(flag), *[_ptr(o) for o in out]),
+          None, "focal_plane_to_sky")
+    return tuple(out)
 
 
 def beam_npix_for_radius(nside: int, radius_rad: float) -> int:
@@ -452,6 +471,18 @@ class GPUConvolver:
                                             ctypes.byref(ch), ctypes.byref(ms)),
               self.ctx, "autotune_batched")
         return int(ch.value), float(ms.value)
+
+    def batched_config(self):
+        """(chunk, warps per block) the batched launch uses now."""
+        ch = ctypes.c_int()
+        w = ctypes.c_int()
+        check(load().pisco_batched_config(self.ctx, ctypes.byref(ch), ctypes.byref(w)), self.ctx,
+              "batched_config")
+        return int(ch.value), int(w.value)
+
+    def set_batched_config(self, chunk: int = 0, warps_per_block: int = 8) -> None:
+        check(load().pisco_set_batched_config(self.ctx, int(chunk), int(warps_per_block)),
+              self.ctx, "set_batched_config")
 
     def tuned_calibrate(self, begin: int = 0, n: int | None = None, with_pairs: bool = False):
         """Worst FP32 decision error of the TUNED form as a fraction of its

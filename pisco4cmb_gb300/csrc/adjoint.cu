@@ -40,12 +40,13 @@ struct Scatter {
     static constexpr bool kStencil = false;  // the sky gradient needs the interpolated value only
     float ga, gb;
     float* gsky;                  // ATOMIC: float4-interleaved [npix][4]
-    unsigned long long* gsky_fx;  // DETERMINISTIC: int64 [npix][4]
+    unsigned long long* gsky_fx;  // DETERMINISTIC: int64 planes [4][npix]
     float* gbeam;                 // ATOMIC: [npixB][8] (a.IQUV, b.IQUV) or null
     unsigned long long* gbeam_fx;
     const float4* sky;            // for the beam gradient
     double ssky, sbeam;           // fixed-point scales 2^S
     int want_v;                   // accumulate the V column
+    long long plane;              // npix: the stride of the fixed-point planes
 
     __device__ __forceinline__ static unsigned long long fx(double v, double scale)
     {
@@ -76,11 +77,13 @@ struct Scatter {
         const float gU = wa * (B.a.z * c2 + B.a.y * s2) + wb * (-B.b.z * c2 - B.b.y * s2);
         const float gV = want_v ? wa * B.a.w + wb * B.b.w : 0.0f;
         if (kFixed) {
-            unsigned long long* p = gsky_fx + 4ll * pix;
-            atomicAdd(p + 0, fx(gI, ssky));
-            atomicAdd(p + 1, fx(gQ, ssky));
-            atomicAdd(p + 2, fx(gU, ssky));
-            if (want_v) atomicAdd(p + 3, fx(gV, ssky));
+            // one plane per Stokes component: the lanes of a warp, on
+            // consecutive pixels of a ring, add to consecutive words
+            unsigned long long* p = gsky_fx + pix;
+            atomicAdd(p, fx(gI, ssky));
+            atomicAdd(p + plane, fx(gQ, ssky));
+            atomicAdd(p + 2 * plane, fx(gU, ssky));
+            if (want_v) atomicAdd(p + 3 * plane, fx(gV, ssky));
         } else {
             atomicAdd(reinterpret_cast<float4*>(gsky) + pix, make_float4(gI, gQ, gU, gV));
         }
@@ -105,6 +108,7 @@ struct ScatterBeam {
     double ssky, sbeam;
     int want_sky;
     int want_v;
+    long long plane;
 
     __device__ __forceinline__ void stash(tuned::Pend& p) const
     {
@@ -159,8 +163,8 @@ struct ScatterBeam {
                                            const F8& B, long long bp, float c2, float s2) const
     {
         if (want_sky) {
-            const Scatter<kFixed> sc{wa,      wb,   gsky,  gsky_fx, nullptr,
-                                     nullptr, nullptr, ssky, sbeam, want_v};
+            const Scatter<kFixed> sc{wa,      wb,      gsky,  gsky_fx, nullptr,
+                                     nullptr, nullptr, ssky,  sbeam,   want_v, plane};
             sc.scatter(wa, wb, pix, B, c2, s2);
         }
         float v[8];
@@ -196,8 +200,8 @@ struct ScatterBeam {
                 B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);
                 B.b.z = fmaf(v.b.z, w[i], B.b.z); B.b.w = fmaf(v.b.w, w[i], B.b.w);
             }
-            const Scatter<kFixed> sc{wa,      wb,   gsky,  gsky_fx, nullptr,
-                                     nullptr, nullptr, ssky, sbeam, want_v};
+            const Scatter<kFixed> sc{wa,      wb,      gsky,  gsky_fx, nullptr,
+                                     nullptr, nullptr, ssky,  sbeam,   want_v, plane};
             sc.scatter(wa, wb, pix, B, c2, s2);
         }
         float v[8];
@@ -429,6 +433,20 @@ __global__ void fixed_to_float_kernel(const unsigned long long* in, void* out, i
     }
 }
 
+// The DETERMINISTIC sky accumulator (planes [4][npix]) to the interleaved
+// [npix][4] gradient.
+__global__ void fixed_planes_kernel(const unsigned long long* in, void* out, int out_f64,
+                                    long long npix, double inv_scale)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 4 * npix;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i >> 2, k = i & 3;
+        const double v = (double)(long long)in[k * npix + p] * inv_scale;
+        if (out_f64) ((double*)out)[i] = v;
+        else ((float*)out)[i] = (float)v;
+    }
+}
+
 template <class K>
 int resident_blocks(K kernel, int threads)
 {
@@ -493,10 +511,19 @@ cudaError_t launch_fold_params(const double* ppart, int nwarps, double* row, cud
     return cudaGetLastError();
 }
 
+cudaError_t launch_fixed_planes_to_float(const unsigned long long* in, void* out, int out_f64,
+                                         long long npix, double inv_scale, cudaStream_t st)
+{
+    if (npix <= 0) return cudaSuccess;
+    fixed_planes_kernel<<<1024, 256, 0, st>>>(in, out, out_f64, npix, inv_scale);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int* nwarps)
 {
     if (nwarps) *nwarps = 0;
     if (a.n <= 0) return cudaSuccess;
+    const long long plane = 12LL * a.nside_sky * a.nside_sky;
     if (a.ptab) {
         if (a.fixed) {
             ScatterParams<true> act{};
@@ -507,7 +534,7 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
             act.ci = a.ceps_i;
             act.cq = a.ceps_q;
             act.sc = Scatter<true>{0,       0,       nullptr,     a.gsky_fx,    nullptr,
-                                   nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v};
+                                   nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v, plane};
             act.want_sky = a.gsky_fx != nullptr;
             return launch_act(a, act, sm_count, st, nwarps);
         }
@@ -518,7 +545,8 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
         act.ppart = a.ppart;
         act.ci = a.ceps_i;
         act.cq = a.ceps_q;
-        act.sc = Scatter<false>{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0, a.want_v};
+        act.sc = Scatter<false>{0,       0,   a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0,
+                                a.want_v, plane};
         act.want_sky = a.gsky32 != nullptr;
         return launch_act(a, act, sm_count, st, nwarps);
     }
@@ -527,11 +555,12 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
         if (beam) {
             ScatterBeam<true> act{0,          0,         a.beam32,     a.sky32,
                                   nullptr,    a.gsky_fx, nullptr,      a.gbeam_fx,
-                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr, a.want_v};
+                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr, a.want_v,
+                                  plane};
             return launch_act(a, act, sm_count, st, nwarps);
         }
         Scatter<true> act{0,       0,       nullptr,     a.gsky_fx,    nullptr,
-                          nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v};
+                          nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v, plane};
         return launch_act(a, act, sm_count, st, nwarps);
     }
     if (beam) {

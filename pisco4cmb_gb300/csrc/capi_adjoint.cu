@@ -306,8 +306,8 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
             CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
         if (d_gsky)
-            CK(launch_fixed_to_float(c->adj_sky_fx, d_gsky, out_dtype == PISCO_FLOAT64, nsky,
-                                     a.sky_scale > 0.0 ? 1.0 / a.sky_scale : 0.0, s),
+            CK(launch_fixed_planes_to_float(c->adj_sky_fx, d_gsky, out_dtype == PISCO_FLOAT64, npix,
+                                            a.sky_scale > 0.0 ? 1.0 / a.sky_scale : 0.0, s),
                "sky gradient");
         if (d_gbeam)
             CK(launch_fixed_to_float(c->adj_beam_fx, d_gbeam, out_dtype == PISCO_FLOAT64, nbeam,

@@ -75,19 +75,26 @@ pisco_status validate(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_
 }
 
 std::string launch_key(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_dtype out_dtype,
-                       int chunk)
+                       int chunk, int warps)
 {
     std::string k((const char*)dets, sizeof(pisco_det_desc) * (size_t)ndet);
     char tail[128];
-    std::snprintf(tail, sizeof tail, "|%d|%d|%p|%d|%d", chunk, (int)out_dtype, (void*)c->sky32,
-                  c->nside_sky, (int)c->interp);
+    std::snprintf(tail, sizeof tail, "|%d|%d|%d|%p|%d|%d", chunk, warps, (int)out_dtype,
+                  (void*)c->sky32, c->nside_sky, (int)c->interp);
     return k + tail;
 }
 
-// ---- a flat JSON object {"key": [chunk, ms], ...} -------------------------
-std::map<std::string, std::pair<int, double>> read_cache(const char* path)
+// One autotuned choice: chunk, warps per block, time.
+struct Tuned {
+    int chunk;
+    int warps;
+    double ms;
+};
+
+// ---- a flat JSON object {"key": [chunk, ms, warps], ...} -------------------
+std::map<std::string, Tuned> read_cache(const char* path)
 {
-    std::map<std::string, std::pair<int, double>> m;
+    std::map<std::string, Tuned> m;
     std::ifstream f(path);
     if (!f) return m;
     std::stringstream ss;
@@ -100,16 +107,17 @@ std::map<std::string, std::pair<int, double>> read_cache(const char* path)
         const std::string key = s.substr(p + 1, q - p - 1);
         const size_t lb = s.find('[', q), rb = s.find(']', q);
         if (lb == std::string::npos || rb == std::string::npos || lb > rb) break;
-        int chunk = 0;
+        int chunk = 0, warps = 8;
         double ms = 0.0;
-        if (std::sscanf(s.c_str() + lb + 1, "%d , %lf", &chunk, &ms) == 2 && chunk > 0)
-            m[key] = {chunk, ms};
+        const int got = std::sscanf(s.c_str() + lb + 1, "%d , %lf , %d", &chunk, &ms, &warps);
+        if (got >= 2 && chunk > 0)
+            m[key] = Tuned{chunk, got == 3 && batched_warps_valid(warps) ? warps : 8, ms};
         p = rb + 1;
     }
     return m;
 }
 
-bool write_cache(const char* path, const std::map<std::string, std::pair<int, double>>& m)
+bool write_cache(const char* path, const std::map<std::string, Tuned>& m)
 {
     const std::string tmp = std::string(path) + ".tmp";
     std::ofstream f(tmp);
@@ -117,7 +125,8 @@ bool write_cache(const char* path, const std::map<std::string, std::pair<int, do
     f << "{\n";
     size_t i = 0;
     for (const auto& kv : m)
-        f << "  \"" << kv.first << "\": [" << kv.second.first << ", " << kv.second.second << "]"
+        f << "  \"" << kv.first << "\": [" << kv.second.chunk << ", " << kv.second.ms << ", "
+          << kv.second.warps << "]"
           << (++i < m.size() ? ",\n" : "\n");
     f << "}\n";
     f.close();
@@ -173,10 +182,11 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
     if (st != PISCO_OK) return st;
     if (chunk < 0) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "chunk must be >= 0");
     if (chunk == 0) chunk = c->batched_chunk > 0 ? c->batched_chunk : 256;
+    const int warps = c->batched_warps;
     st = c->activate();
     if (st != PISCO_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-    const std::string key = launch_key(c, dets, ndet, out_dtype, chunk);
+    const std::string key = launch_key(c, dets, ndet, out_dtype, chunk, warps);
     if (!(c->graph_exec && key == c->graph_key)) {
         // the descriptors, items and orders below may still be read by the
         // previous launch (on another stream)
@@ -241,7 +251,9 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned int), c->stream);
-        cudaError_t e2 = e1 == cudaSuccess ? launch_batched(a, batched_grid(c->sm_count), c->stream) : e1;
+        cudaError_t e2 = e1 == cudaSuccess
+                             ? launch_batched(a, batched_grid(c->sm_count, warps), c->stream, warps)
+                             : e1;
         cudaError_t e3 = cudaStreamEndCapture(c->stream, &g);
         if (e2 != cudaSuccess || e3 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -258,6 +270,25 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
     CK(cudaGraphLaunch(c->graph_exec, s), "graph launch");
     if (!c->batch_event) CK(cudaEventCreateWithFlags(&c->batch_event, cudaEventDisableTiming), "event");
     CK(cudaEventRecord(c->batch_event, s), "batch event");
+    return PISCO_OK;
+}
+
+pisco_status pisco_batched_config(pisco_ctx* c, int* chunk, int* warps_per_block)
+{
+    if (!c) return PISCO_ERR_INVALID_ARGUMENT;
+    if (chunk) *chunk = c->batched_chunk > 0 ? c->batched_chunk : 256;
+    if (warps_per_block) *warps_per_block = c->batched_warps;
+    return PISCO_OK;
+}
+
+pisco_status pisco_set_batched_config(pisco_ctx* c, int chunk, int warps_per_block)
+{
+    if (!c) return PISCO_ERR_INVALID_ARGUMENT;
+    if (chunk < 0) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "chunk must be >= 0");
+    if (!batched_warps_valid(warps_per_block))
+        return fail(c, PISCO_ERR_INVALID_ARGUMENT, "warps per block must be 4, 8 or 16");
+    if (chunk > 0) c->batched_chunk = chunk;
+    c->batched_warps = warps_per_block;
     return PISCO_OK;
 }
 
@@ -288,51 +319,63 @@ pisco_status pisco_autotune_batched(pisco_ctx* c, const pisco_det_desc* dets, in
         }
     }
     char key[512];
-    std::snprintf(key, sizeof key, "%s|nside_sky=%d|ndet=%d|beams=%016llx|log2n=%d|%s|tuned",
+    std::snprintf(key, sizeof key, "%s|nside_sky=%d|ndet=%d|beams=%016llx|log2n=%d|%s|%s|tuned",
                   prop.name, c->nside_sky, ndet, h, (int)std::log2((double)std::max<long long>(total, 1)),
-                  out_dtype == PISCO_FLOAT64 ? "f64" : "f32");
-    std::map<std::string, std::pair<int, double>> cache;
+                  out_dtype == PISCO_FLOAT64 ? "f64" : "f32",
+                  c->interp == PISCO_BEAM_BILINEAR ? "bilinear" : "nearest");
+    std::map<std::string, Tuned> cache;
     if (cache_path) {
         cache = read_cache(cache_path);
         auto it = cache.find(key);
         if (it != cache.end()) {
-            c->batched_chunk = it->second.first;
-            if (chunk_out) *chunk_out = it->second.first;
-            if (ms_out) *ms_out = it->second.second;
+            c->batched_chunk = it->second.chunk;
+            c->batched_warps = it->second.warps;
+            if (chunk_out) *chunk_out = it->second.chunk;
+            if (ms_out) *ms_out = it->second.ms;
             return PISCO_OK;
         }
     }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
-    int best = 256;
+    int best = 256, best_w = 8;
     double best_ms = 1e300;
-    for (int chunk : {32, 64, 128, 256, 512, 1024, 2048, 4096, 8192}) {
-        st = pisco_forward_batched(c, dets, ndet, out_dtype, chunk, c->stream);  // warm-up + capture
+    const int keep_w = c->batched_warps;
+    for (int warps : {8, 16, 4}) {
+        c->batched_warps = warps;
+        for (int chunk : {32, 64, 128, 256, 512, 1024, 2048, 4096, 8192}) {
+            st = pisco_forward_batched(c, dets, ndet, out_dtype, chunk, c->stream);  // warm-up + capture
+            if (st != PISCO_OK) break;
+            double ms = 1e300;
+            for (int rep = 0; rep < 2 && st == PISCO_OK; ++rep) {
+                cudaEventRecord(e0, c->stream);
+                st = pisco_forward_batched(c, dets, ndet, out_dtype, chunk, c->stream);
+                cudaEventRecord(e1, c->stream);
+                cudaEventSynchronize(e1);
+                float t = 0.0f;
+                cudaEventElapsedTime(&t, e0, e1);
+                ms = std::min(ms, (double)t);
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = chunk;
+                best_w = warps;
+            }
+        }
         if (st != PISCO_OK) break;
-        double ms = 1e300;
-        for (int rep = 0; rep < 2 && st == PISCO_OK; ++rep) {
-            cudaEventRecord(e0, c->stream);
-            st = pisco_forward_batched(c, dets, ndet, out_dtype, chunk, c->stream);
-            cudaEventRecord(e1, c->stream);
-            cudaEventSynchronize(e1);
-            float t = 0.0f;
-            cudaEventElapsedTime(&t, e0, e1);
-            ms = std::min(ms, (double)t);
-        }
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = chunk;
-        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (st != PISCO_OK) return st;
+    if (st != PISCO_OK) {
+        c->batched_warps = keep_w;
+        return st;
+    }
     st = c->check_device();
     if (st != PISCO_OK) return st;
     c->batched_chunk = best;
+    c->batched_warps = best_w;
     if (cache_path) {
-        cache[key] = {best, best_ms};
+        cache[key] = Tuned{best, best_w, best_ms};
         if (!write_cache(cache_path, cache))
             return fail(c, PISCO_ERR_INVALID_ARGUMENT, std::string("cannot write ") + cache_path);
     }

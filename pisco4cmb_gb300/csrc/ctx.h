@@ -100,6 +100,7 @@ struct pisco_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::string graph_key;
     int batched_chunk = 0;  // last autotuned chunk (0 = not tuned)
+    int batched_warps = 8;  // warps per block of the batched kernel (autotuned)
 
     // adjoint scratch
     float* adj_sky32 = nullptr;

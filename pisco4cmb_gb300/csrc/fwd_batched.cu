@@ -9,9 +9,9 @@
 // and one kernel whose blocks pull chunks with one atomic each runs them all
 // (the warps of a block share a chunk, sample by sample).
 // The launch (queue reset + kernel) is captured once in a CUDA graph and
-// replayed while the same detector set is resubmitted.  The chunk size is
-// chosen by the autotuner (pisco_autotune_batched) and cached per workload
-// key in a JSON file.
+// replayed while the same detector set is resubmitted.  The chunk size and
+// the block shape (warps per block) are chosen by the autotuner
+// (pisco_autotune_batched) and cached per workload key in a JSON file.
 //
 // Per sample the TUNED geometry of tuned_core.cuh runs unchanged, so every
 // detector's TOD equals its single-detector TUNED forward bit for bit.
@@ -35,7 +35,6 @@ using namespace pisco;
 namespace pisco {
 namespace {
 
-constexpr int kBW = PISCO_TUNED_WARPS;  // warps per block
 
 // A block pulls one item at a time and its warps take the item's samples
 // round-robin, so the warps of an SM work on neighbouring samples (whose
@@ -54,10 +53,14 @@ struct ItemState {
     int state;  // 0: queue empty, 1: run, 2: bad item (skipped)
 };
 
-// kBil: bilinear beam lookup (tuned_core.cuh bilinear_f32).
-template <bool kBil>
-__global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(BatchArgs a)
+// kBil: bilinear beam lookup (tuned_core.cuh bilinear_f32).  kW: warps per
+// block, the tile the autotuner picks with the chunk size; every shape keeps
+// 16 warps per SM (16 / kW blocks), so all compile to the same 128-register
+// cap and differ in how many warps share an item (and its samples' discs).
+template <bool kBil, int kW>
+__global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
 {
+    constexpr int kBW = kW;
     __shared__ tuned::WarpSmem sm[kBW];
     __shared__ ItemState s_item[2];
     const int lane = threadIdx.x & 31;
@@ -114,21 +117,41 @@ __global__ void __launch_bounds__(kBW * 32, PISCO_TUNED_MINB) batched_kernel(Bat
 
 }  // namespace
 
-int batched_grid(int sm_count)
+namespace {
+
+template <int kW>
+int grid_of(int sm_count)
 {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false>, kBW * 32, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false, kW>, kW * 32, 0) !=
             cudaSuccess ||
         nb < 1)
         nb = 1;
     return sm_count * nb;
 }
 
-cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st)
+template <int kW>
+void launch_shape(const BatchArgs& a, int grid, cudaStream_t st)
+{
+    if (a.interp == 1) batched_kernel<true, kW><<<grid, kW * 32, 0, st>>>(a);
+    else batched_kernel<false, kW><<<grid, kW * 32, 0, st>>>(a);
+}
+
+}  // namespace
+
+bool batched_warps_valid(int warps) { return warps == 4 || warps == 8 || warps == 16; }
+
+int batched_grid(int sm_count, int warps)
+{
+    return warps == 4 ? grid_of<4>(sm_count) : warps == 16 ? grid_of<16>(sm_count) : grid_of<8>(sm_count);
+}
+
+cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st, int warps)
 {
     if (a.nitems <= 0) return cudaSuccess;
-    if (a.interp == 1) batched_kernel<true><<<grid, kBW * 32, 0, st>>>(a);
-    else batched_kernel<false><<<grid, kBW * 32, 0, st>>>(a);
+    if (warps == 4) launch_shape<4>(a, grid, st);
+    else if (warps == 16) launch_shape<16>(a, grid, st);
+    else launch_shape<8>(a, grid, st);
     return cudaGetLastError();
 }
 

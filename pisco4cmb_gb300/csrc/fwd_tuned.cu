@@ -14,11 +14,23 @@
 namespace pisco {
 namespace {
 
-constexpr int kTW = PISCO_TUNED_WARPS;
+// The single-detector forward runs one block of 16 warps per SM (register
+// cap 128, the same as 8 warps x 2 blocks): the 16 warps of an SM then work on
+// 16 consecutive samples, whose discs overlap, instead of two groups of 8
+// far apart, so their sky reads share L1 (c2 forward: 174.3 ms against
+// 176.2 ms for 8 x 2 and 178.7 ms for 4 x 4).  Its 83 KB of per-warp shared
+// state is a static allocation, which sm_103a allows beyond 48 KB.
+#ifndef PISCO_FWD_WARPS
+#define PISCO_FWD_WARPS 16
+#endif
+#ifndef PISCO_FWD_MINB
+#define PISCO_FWD_MINB 1
+#endif
+constexpr int kTW = PISCO_FWD_WARPS;
 
 // kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
 template <bool kCalib, bool kBil>
-__global__ void __launch_bounds__(kTW * 32, PISCO_TUNED_MINB)
+__global__ void __launch_bounds__(kTW * 32, PISCO_FWD_MINB)
     tuned_kernel(FwdArgs a, float* calib)
 {
     __shared__ tuned::WarpSmem sm[kTW];

@@ -136,7 +136,7 @@ struct AdjArgs {
     int g_f64;
     int fixed;                     // 1: fixed-point int64 accumulation
     float* gsky32;                 // atomic: [npix][4] or null
-    unsigned long long* gsky_fx;   // fixed: [npix][4] or null
+    unsigned long long* gsky_fx;   // fixed: planes [4][npix] or null
     float* gbeam32;                // atomic: [npixB][8] or null
     unsigned long long* gbeam_fx;  // fixed: [npixB][8] or null
     double sky_scale, beam_scale;  // fixed-point scales 2^S
@@ -201,6 +201,9 @@ cudaError_t launch_abs_sum(const void* ga, const void* gb, int f64, long long n,
 cudaError_t launch_abs_max(const float* x, long long n, double* part, cudaStream_t st);
 cudaError_t launch_fixed_to_float(const unsigned long long* in, void* out, int out_f64, long long n,
                                   double inv_scale, cudaStream_t st);
+// The sky's fixed-point planes [4][npix] to the interleaved [npix][4] gradient.
+cudaError_t launch_fixed_planes_to_float(const unsigned long long* in, void* out, int out_f64,
+                                         long long npix, double inv_scale, cudaStream_t st);
 
 // PLAIN (f64 = false) and FP64 (f64 = true) forms.
 cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaStream_t st);
@@ -221,8 +224,10 @@ cudaError_t sky_order(long long n, const double* ra, const double* dec, unsigned
 // Fills the sky ring table (4 nside - 1 entries) for nside <= 8192.
 cudaError_t launch_ring_table(int nside, RingT* rings, cudaStream_t st);
 // Batched TUNED forward (fwd_batched.cu).
-int batched_grid(int sm_count);
-cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st);
+// warps: warps per block, 4, 8 or 16 (16 warps per SM in every shape).
+bool batched_warps_valid(int warps);
+int batched_grid(int sm_count, int warps = 8);
+cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st, int warps = 8);
 // Per-sample disc sizes (pairs) for the roofline byte model.
 cudaError_t launch_count_pairs(int nside_sky, double rho_max, long long n, const double* ra,
                                const double* dec, unsigned long long* total, int sm_count,

@@ -238,10 +238,14 @@ __device__ __forceinline__ float rcp_approx(float x)
 }
 
 // One beam pixel, both detectors (32 bytes, one sector): a single 256-bit
-// load through the read-only path (PISCO_BEAM_LOAD 0: the compiler's own
-// loads, two 128-bit ones).
+// load through the read-only path that does not allocate in L1, so the
+// scattered beam reads (a beam of 10^4 - 10^6 pixels, L2-resident) leave L1
+// to the sky pixels, which neighbouring samples re-read (measured on the
+// c2 forward: 176.2 ms against 177.2 ms allocating in L1).  PISCO_BEAM_LOAD
+// 0: the compiler's own loads (two 128-bit ones); 1: 256-bit, allocating in
+// L1; 3: 256-bit, L2 only (.cg).
 #ifndef PISCO_BEAM_LOAD
-#define PISCO_BEAM_LOAD 1
+#define PISCO_BEAM_LOAD 2
 #endif
 __device__ __forceinline__ F8 load_beam(const F8* p)
 {

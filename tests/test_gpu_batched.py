@@ -114,16 +114,42 @@ def test_batched_chunk_sizes_agree(gpu):
             assert np.array_equal(x, y)
 
 
+def test_batched_tiles_agree(gpu):
+    """Every block shape (4, 8, 16 warps per block) gives the same TOD bit for
+    bit: each sample's result does not depend on which warp runs it."""
+    from pisco4cmb_gb300 import PiscoInvalidArgument
+
+    conv, dets, beams, host, *_ = _setup(ndet=4, seed=13)
+    descs = conv.det_descs(dets)
+    res = []
+    for warps in (8, 4, 16):
+        conv.set_batched_config(128, warps)
+        assert conv.batched_config() == (128, warps)
+        conv.forward_batched(descs)
+        conv.sync()
+        res.append([o.cpu().numpy().copy() for h in host for o in h["outs"]])
+    for r in res[1:]:
+        for x, y in zip(res[0], r):
+            assert np.array_equal(x, y)
+    with pytest.raises(PiscoInvalidArgument):
+        conv.set_batched_config(0, 12)
+
+
 def test_autotune_and_cache(gpu, tmp_path):
     conv, dets, *_ = _setup(ndet=5, seed=9)
     descs = conv.det_descs(dets)
     path = str(tmp_path / "tune.json")
     chunk, ms = conv.autotune_batched(descs, cache_path=path)
     assert chunk in (32, 64, 128, 256, 512, 1024, 2048, 4096, 8192) and ms > 0
+    _, warps = conv.batched_config()
+    assert warps in (4, 8, 16)
     data = json.load(open(path))
     assert len(data) == 1 and list(data.values())[0][0] == chunk
+    assert list(data.values())[0][2] == warps
+    conv.set_batched_config(64, 8 if warps != 8 else 4)
     chunk2, ms2 = conv.autotune_batched(descs, cache_path=path)  # served from the cache
     assert (chunk2, ms2) == (chunk, list(data.values())[0][1])
+    assert conv.batched_config() == (chunk, warps)
     conv.forward_batched(descs)  # chunk 0 = the tuned value
     conv.sync()
 
