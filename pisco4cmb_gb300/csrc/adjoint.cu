@@ -44,13 +44,17 @@ struct Scatter {
     float* gbeam;                 // ATOMIC: [npixB][8] (a.IQUV, b.IQUV) or null
     unsigned long long* gbeam_fx;
     const float4* sky;            // for the beam gradient
-    double ssky, sbeam;           // fixed-point scales 2^S
+    float ssky, sbeam;            // fixed-point scales 2^S (at most 2^126)
     int want_v;                   // accumulate the V column
     long long plane;              // npix: the stride of the fixed-point planes
 
-    __device__ __forceinline__ static unsigned long long fx(double v, double scale)
+    // v 2^S rounded to the nearest integer.  The scale is a power of two, so
+    // the FP32 product is exact and the FP32 -> int64 conversion gives what
+    // the FP64 route would, without two FP64 instructions per component (the
+    // FP64 pipe of this GPU issues a small fraction of the FP32 rate).
+    __device__ __forceinline__ static unsigned long long fx(float v, float scale)
     {
-        return (unsigned long long)__double2ll_rn(v * scale);
+        return (unsigned long long)__float2ll_rn(v * scale);
     }
 
     __device__ __forceinline__ void stash(tuned::Pend& p) const
@@ -105,7 +109,7 @@ struct ScatterBeam {
     unsigned long long* gsky_fx;
     float* gbeam;
     unsigned long long* gbeam_fx;
-    double ssky, sbeam;
+    float ssky, sbeam;
     int want_sky;
     int want_v;
     long long plane;
@@ -524,6 +528,8 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
     if (nwarps) *nwarps = 0;
     if (a.n <= 0) return cudaSuccess;
     const long long plane = 12LL * a.nside_sky * a.nside_sky;
+    // fixed-point scales: powers of two of at most 2^126, exact in FP32
+    const float fsky = (float)a.sky_scale, fbeam = (float)a.beam_scale;
     if (a.ptab) {
         if (a.fixed) {
             ScatterParams<true> act{};
@@ -534,7 +540,7 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
             act.ci = a.ceps_i;
             act.cq = a.ceps_q;
             act.sc = Scatter<true>{0,       0,       nullptr,     a.gsky_fx,    nullptr,
-                                   nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v, plane};
+                                   nullptr, a.sky32, fsky, fbeam, a.want_v, plane};
             act.want_sky = a.gsky_fx != nullptr;
             return launch_act(a, act, sm_count, st, nwarps);
         }
@@ -545,7 +551,7 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
         act.ppart = a.ppart;
         act.ci = a.ceps_i;
         act.cq = a.ceps_q;
-        act.sc = Scatter<false>{0,       0,   a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0,
+        act.sc = Scatter<false>{0,       0,   a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0f, 0.0f,
                                 a.want_v, plane};
         act.want_sky = a.gsky32 != nullptr;
         return launch_act(a, act, sm_count, st, nwarps);
@@ -555,21 +561,21 @@ cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int*
         if (beam) {
             ScatterBeam<true> act{0,          0,         a.beam32,     a.sky32,
                                   nullptr,    a.gsky_fx, nullptr,      a.gbeam_fx,
-                                  a.sky_scale, a.beam_scale, a.gsky_fx != nullptr, a.want_v,
+                                  fsky, fbeam, a.gsky_fx != nullptr, a.want_v,
                                   plane};
             return launch_act(a, act, sm_count, st, nwarps);
         }
         Scatter<true> act{0,       0,       nullptr,     a.gsky_fx,    nullptr,
-                          nullptr, a.sky32, a.sky_scale, a.beam_scale, a.want_v, plane};
+                          nullptr, a.sky32, fsky, fbeam, a.want_v, plane};
         return launch_act(a, act, sm_count, st, nwarps);
     }
     if (beam) {
         ScatterBeam<false> act{0,         0,       a.beam32, a.sky32, a.gsky32,
-                               nullptr,   a.gbeam32, nullptr, 0.0,   0.0,
+                               nullptr,   a.gbeam32, nullptr, 0.0f,  0.0f,
                                a.gsky32 != nullptr, a.want_v};
         return launch_act(a, act, sm_count, st, nwarps);
     }
-    Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0, 0.0, a.want_v};
+    Scatter<false> act{0, 0, a.gsky32, nullptr, nullptr, nullptr, a.sky32, 0.0f, 0.0f, a.want_v};
     return launch_act(a, act, sm_count, st, nwarps);
 }
 

@@ -2,6 +2,7 @@
 // and of the device-side beam setter used by the autograd binding.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -62,11 +63,13 @@ __global__ void widen_f32(const float* in, double* out, long long n)
 }
 
 // smallest power of two >= 2^62 / bound, as the fixed-point scale
+// (at most 2^126, so that the kernels can apply it in FP32; a bound below
+// 2^-64 keeps every total far below 2^62 all the same)
 double fixed_scale(double bound)
 {
     if (!(bound > 0.0) || !std::isfinite(bound)) return 0.0;
     const int e = (int)std::ceil(std::log2(bound));
-    return std::ldexp(1.0, 62 - e);
+    return std::ldexp(1.0, std::min(62 - e, 126));
 }
 
 // The fused Gaussian beam-parameter gradient of one adjoint call: the model
