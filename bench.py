@@ -64,6 +64,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def ncu_l2_bytes_per_pair():
+    """L2 bytes served per (sample, disc pixel) pair by the tuned forward, from
+    the committed ncu summary (line 'l2_bytes_per_pair: <float>')."""
+    p = os.path.join(ROOT, "profiles", "tuned_forward_c2_ncu.md")
+    if os.path.exists(p):
+        with open(p) as f:
+            for line in f:
+                if line.strip().startswith("l2_bytes_per_pair:"):
+                    return float(line.split(":", 1)[1].strip())
+    return None
+
+
 def ncu_traffic_per_launch():
     """DRAM bytes (read + write) per full-size launch of the tuned forward, from
     the committed ncu summary (line 'dram_bytes_per_launch: <int>')."""
@@ -402,6 +414,13 @@ def run_gpu_arm(args, rank, world, local):
     alg_bytes = pairs * BYTES_PER_PAIR + n * BYTES_PER_SAMPLE
     achieved = alg_bytes / (t_total / args.steps) / 1e9
     traffic = ncu_traffic_per_launch()
+    # what actually limits the kernel: one dependent L2 gather (the beam) per
+    # pair; L2 bytes per pair from ncu, the rate from this run's time
+    l2_pp = ncu_l2_bytes_per_pair()
+    l2_line = None if l2_pp is None else {
+        "bytes_per_pair": l2_pp, "achieved_gbs": pairs * l2_pp / (t_total / args.steps) / 1e9,
+        "l1_serves": "the sky reads (all hits)", "l2_serves": "the beam gather (all L1 misses)",
+        "source": "profiles/tuned_forward_c2_ncu.md"}
 
     line = None
     if rank == 0:
@@ -430,7 +449,8 @@ def run_gpu_arm(args, rank, world, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic,
-                         "bytes_model": "48 B/pair x exact disc pairs + 32 B/sample"},
+                         "bytes_model": "48 B/pair x exact disc pairs + 32 B/sample",
+                         "l2": l2_line},
             "plain": {"value": plain_sps, "unit": "samples/s", "sample": m_plain,
                       "tuned_over_plain": value / world / plain_sps},
             "accuracy": {"rms_err_vs_fp64": rms_err, "max_err_vs_fp64": max_err,

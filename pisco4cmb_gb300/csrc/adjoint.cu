@@ -198,7 +198,7 @@ struct ScatterBeam {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 if (w[i] == 0.0f) continue;
-                const F8 v = tuned::load_beam(beam_base + px[i]);
+                const F8 v = tuned::load_beam_stencil(beam_base + px[i]);
                 B.a.x = fmaf(v.a.x, w[i], B.a.x); B.a.y = fmaf(v.a.y, w[i], B.a.y);
                 B.a.z = fmaf(v.a.z, w[i], B.a.z); B.a.w = fmaf(v.a.w, w[i], B.a.w);
                 B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);
@@ -283,7 +283,7 @@ struct ScatterParams {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 if (w[i] == 0.0f) continue;
-                const F8 v = tuned::load_beam(beam_base + px[i]);
+                const F8 v = tuned::load_beam_stencil(beam_base + px[i]);
                 B.a.x = fmaf(v.a.x, w[i], B.a.x); B.a.y = fmaf(v.a.y, w[i], B.a.y);
                 B.a.z = fmaf(v.a.z, w[i], B.a.z); B.a.w = fmaf(v.a.w, w[i], B.a.w);
                 B.b.x = fmaf(v.b.x, w[i], B.b.x); B.b.y = fmaf(v.b.y, w[i], B.b.y);

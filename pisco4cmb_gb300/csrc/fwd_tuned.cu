@@ -14,23 +14,26 @@
 namespace pisco {
 namespace {
 
-// The single-detector forward runs one block of 16 warps per SM (register
-// cap 128, the same as 8 warps x 2 blocks): the 16 warps of an SM then work on
-// 16 consecutive samples, whose discs overlap, instead of two groups of 8
-// far apart, so their sky reads share L1 (c2 forward: 174.3 ms against
-// 176.2 ms for 8 x 2 and 178.7 ms for 4 x 4).  Its 83 KB of per-warp shared
-// state is a static allocation, which sm_103a allows beyond 48 KB.
+// Launch shape: the nearest lookup runs one block of 16 warps per SM
+// (register cap 128, the same as 8 warps x 2 blocks): the 16 warps of an SM
+// then work on 16 consecutive samples, whose discs overlap, instead of two
+// groups of 8 far apart, so their sky reads share L1 (c2 forward: 174.8 ms
+// against 176.7 ms for 8 x 2 and 178.7 ms for 4 x 4).  Its 83 KB of per-warp
+// shared state is a static allocation, which sm_103a allows beyond 48 KB.
+// The bilinear lookup, whose four stencil reads per pair want L1 for
+// themselves, runs 8 x 2 (348.4 ms against 368.5 ms for 16 x 1, both with
+// one allocating 256-bit load per stencil pixel).
 #ifndef PISCO_FWD_WARPS
 #define PISCO_FWD_WARPS 16
 #endif
-#ifndef PISCO_FWD_MINB
-#define PISCO_FWD_MINB 1
+#ifndef PISCO_BIL_WARPS
+#define PISCO_BIL_WARPS 8
 #endif
-constexpr int kTW = PISCO_FWD_WARPS;
 
 // kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
-template <bool kCalib, bool kBil>
-__global__ void __launch_bounds__(kTW * 32, PISCO_FWD_MINB)
+// kTW: warps per block (16 / kTW blocks per SM).
+template <bool kCalib, bool kBil, int kTW>
+__global__ void __launch_bounds__(kTW * 32, 16 / kTW)
     tuned_kernel(FwdArgs a, float* calib)
 {
     __shared__ tuned::WarpSmem sm[kTW];
@@ -99,22 +102,23 @@ int resident_blocks(K kernel, int threads)
     return nb;
 }
 
+template <bool kCalib, bool kBil, int kTW>
+void launch_shape(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib)
+{
+    const int threads = kTW * 32;
+    const long long need = (a.n + kTW - 1) / kTW;
+    const long long blocks =
+        (long long)sm_count * resident_blocks(tuned_kernel<kCalib, kBil, kTW>, threads);
+    tuned_kernel<kCalib, kBil, kTW><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, calib);
+}
+
 cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib)
 {
     if (a.n <= 0) return cudaSuccess;
-    const int threads = kTW * 32;
-    const long long need = (a.n + kTW - 1) / kTW;
     // calibration measures the nearest-pixel decisions, whatever the lookup
-    if (calib) {
-        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<true, false>, threads);
-        tuned_kernel<true, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, calib);
-    } else if (a.interp == 1) {
-        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, true>, threads);
-        tuned_kernel<false, true><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, nullptr);
-    } else {
-        long long blocks = (long long)sm_count * resident_blocks(tuned_kernel<false, false>, threads);
-        tuned_kernel<false, false><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, nullptr);
-    }
+    if (calib) launch_shape<true, false, PISCO_FWD_WARPS>(a, sm_count, st, calib);
+    else if (a.interp == 1) launch_shape<false, true, PISCO_BIL_WARPS>(a, sm_count, st, nullptr);
+    else launch_shape<false, false, PISCO_FWD_WARPS>(a, sm_count, st, nullptr);
     return cudaGetLastError();
 }
 

@@ -97,6 +97,39 @@ def test_c2_shape_against_oracle(gpu, oracle_mod):
     _check_forms(oracle_mod, nss, sky, beam, ra[idx], dec[idx], pa[idx])
 
 
+def test_c2_shape_bilinear_against_oracle(gpu, oracle_mod):
+    """The bilinear beam lookup at the c2 shape: TUNED (FP32 stencil) and the
+    FP64 form against the oracle's FP64 get_interpol lookup.  The FP64 form's
+    stencil weights differ from the oracle's by up to ~1e-9 next to the
+    boresight (acos of a cosine near 1 amplifies last-bit differences of the
+    device and host sin/cos), hence 1e-10 of the TOD rms rather than 1e-12."""
+    from pisco4cmb_gb300 import GPUConvolver, Scan, Sky, synth
+
+    O = oracle_mod
+    nss = 1024
+    sky = synth.grf_sky(nss, 2, lmax=LMAX, dtype=np.float32, device="cuda")[:3]
+    beam = _beam(2048, 3.0, 1.5, 0.05, nss)
+    ra, dec, pa = synth.sweep_scan(2_000_000, 2)
+    idx = np.r_[0:500, np.linspace(500, 2_000_000 - 1, 500).astype(np.int64)]
+    ra, dec, pa = ra[idx], dec[idx], pa[idx]
+    ba, bb = beam.planes()
+    oa, ob = O.convolve_f64(ra, dec, pa, nss, sky.astype(np.float64), beam.nside,
+                            ba.astype(np.float64), bb.astype(np.float64), interp=1)
+    for form, rms_tol, max_tol in (("tuned", 1e-6, 1e-5), ("fp64", 1e-10, 1e-10)):
+        c = GPUConvolver(form=form)
+        c.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+        c.update_beam(beam)
+        c.set_interp(True)
+        c.update_scan(Scan(ra.size, ra, dec, pa))
+        a = np.empty(ra.size)
+        b = np.empty(ra.size)
+        c.exec_convolution(a, b)
+        c.close()
+        for g, o in ((a, oa), (b, ob)):
+            assert rel_rms(g, o) <= rms_tol, (form, rel_rms(g, o))
+            assert rel_max(g, o) <= max_tol, (form, rel_max(g, o))
+
+
 def test_c3_shape_pole_heavy_against_oracle(gpu, oracle_mod):
     from pisco4cmb_gb300 import synth
 
