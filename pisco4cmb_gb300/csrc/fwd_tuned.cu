@@ -36,7 +36,10 @@ template <bool kCalib, bool kBil, int kTW>
 __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
     tuned_kernel(FwdArgs a, float* calib)
 {
+    // the nearest lookup stages its sky and beam reads (tuned::StagedGather)
+    constexpr bool kStage = !kBil && !kCalib && PISCO_STAGE != 0;
     __shared__ tuned::WarpSmem sm[kTW];
+    __shared__ float4 stg[kStage ? kTW * tuned::kStageF4 : 1];
     const int lane = threadIdx.x & 31;
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
     const Hpx hs = hpx_make(a.nside_sky);
@@ -46,8 +49,9 @@ __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
     const long long nw = (long long)gridDim.x * kTW;
     unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
-    tuned::Gather g;
+    std::conditional_t<kStage, tuned::StagedGather, tuned::Gather> g;
     g.sky = a.sky32;
+    if constexpr (kStage) g.stage = stg + (threadIdx.x >> 5) * tuned::kStageF4;
     tuned::Queue Q{0, 0};
     for (long long i = gw; i < a.n; i += nw) {
         const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i

@@ -88,6 +88,12 @@ template <class A, class = void>
 struct HasOutside : std::false_type {};
 template <class A>
 struct HasOutside<A, std::void_t<decltype(&A::outside)>> : std::true_type {};
+// Does the action stage its per-pair reads with asynchronous copies
+// (issue / consume, below)?
+template <class A, class = void>
+struct HasStage : std::false_type {};
+template <class A>
+struct HasStage<A, std::void_t<decltype(&A::issue)>> : std::true_type {};
 // Decisions whose FP32 value lies within kMarginRel * (value + 1) of an
 // integer are redone in FP64 (about 20 FP32 ulps).  The observed worst case
 // over a workload is measured by pisco_tuned_calibrate and must stay well
@@ -235,6 +241,29 @@ __device__ __forceinline__ float rcp_approx(float x)
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+}
+
+// 16-byte asynchronous copies global -> this thread's shared memory
+// (cp.async, sm_80 and later): .cg caches in L2 only, .ca in L1 too.  A
+// thread sees the data after its own cp.async.wait_group.
+__device__ __forceinline__ void cp_async_cg16(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_ca16(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // One beam pixel, both detectors (32 bytes, one sector): a single 256-bit
@@ -673,6 +702,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                                        unsigned long long& nfall, float& cmax,
                                        unsigned long long& npairs)
 {
+    constexpr bool kStaged = HasStage<Action>::value && !kBil && !kCalib;
     RingC* W = S.r;
     const unsigned lt_mask = (1u << lane) - 1u;
     Frame F;
@@ -797,10 +827,17 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
         if (lane == 0) npairs += (unsigned long long)total;
         int k = 0;  // lane slot (ring) owning the current pair; only moves forward
         const int iters = (total + 31) >> 5;
+        // staged action: the reads of iteration it are copied while the
+        // geometry of iteration it + 1 runs, and summed after it, so each
+        // lane's sums keep their order
+        [[maybe_unused]] bool pprev = false;
+        [[maybe_unused]] float c2prev = 0.0f, s2prev = 0.0f;
         for (int it = 0; it < iters; ++it) {
             const int t = (it << 5) + lane;
             bool fb = false;
             int pix = 0;
+            [[maybe_unused]] bool pnow = false;
+            [[maybe_unused]] float c2now = 0.0f, s2now = 0.0f;
             if (t < total) {
                 while (W[k].incl <= t) ++k;
                 const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
@@ -917,13 +954,32 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                             if (bp >= 0 && bp < B.npix) {
                                 float c2, s2;
                                 phasor(c2, s2);
-                                act.pair(pix, act.fetch(pix), load_beam(B.beam + bp), bp, c2, s2);
+                                if constexpr (kStaged) {
+                                    act.issue(it & 1, lane, pix, B.beam + bp);
+                                    pnow = true;
+                                    c2now = c2;
+                                    s2now = s2;
+                                } else {
+                                    act.pair(pix, act.fetch(pix), load_beam(B.beam + bp), bp, c2,
+                                             s2);
+                                }
                             } else if constexpr (HasOutside<Action>::value) {
                                 act.outside(pix, bp);
                             }
                         }
                     }
                 }
+            }
+            if constexpr (kStaged) {
+                cp_async_commit();
+                if (it > 0) {
+                    cp_async_wait<1>();
+                    if (pprev) act.consume((it - 1) & 1, lane, c2prev, s2prev);
+                }
+                act.advance();
+                pprev = pnow;
+                c2prev = c2now;
+                s2prev = s2now;
             }
             // queue near-edge pairs; redo them 32 at a time in FP64
             const unsigned mk = __ballot_sync(kFull, fb);
@@ -941,6 +997,10 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
                 __syncwarp();
                 if (Qs.n >= 32) drain<kBil>(hs, 32, S, Qs, lane, err, act);
             }
+        }
+        if constexpr (kStaged) {
+            cp_async_wait<0>();
+            if (pprev) act.consume((iters - 1) & 1, lane, c2prev, s2prev);
         }
         __syncwarp();
     }
@@ -999,6 +1059,51 @@ struct Gather {
             a += __shfl_xor_sync(kFull, a, o);
             b += __shfl_xor_sync(kFull, b, o);
         }
+    }
+};
+
+// Forward action with the sky and beam reads staged through this warp's
+// shared memory by asynchronous copies (two buffers: the pair of iteration
+// it is copied while iteration it + 1 computes its geometry; TOD
+// bit-identical).  PISCO_STAGE 1: sky and beam copied; 2: beam copied, sky
+// loaded into registers; 0 (default): not staged.  Measured on the c2
+// forward (2M samples): 194.2 ms staged, 193.2 ms beam only, against
+// 174.9 ms unstaged -- the three copies, the wait and the three shared-memory
+// reads per pair cost more issue slots than the hidden L2 latency saves
+// (the same with 8 in-flight samples per warp, which keeps the block's
+// shared memory, and so L1, at its unstaged size: 194.0 / 194.3 ms).
+#ifndef PISCO_STAGE
+#define PISCO_STAGE 0
+#endif
+constexpr int kStageRows = PISCO_STAGE == 2 ? 2 : 3;
+// float4 per warp: [buffer][row: beam a, beam b, sky][lane]
+constexpr int kStageF4 = 2 * kStageRows * 32;
+
+struct StagedGather : Gather {
+    float4* stage;  // this warp's kStageF4 float4
+    float4 sk_cur, sk_prev;
+    __device__ __forceinline__ void issue(int buf, int lane, int pix, const F8* bp)
+    {
+        float4* d = stage + buf * (kStageRows * 32) + lane;
+        cp_async_cg16(d, &bp->a);
+        cp_async_cg16(d + 32, &bp->b);
+        if constexpr (kStageRows == 3) cp_async_ca16(d + 64, &sky[pix]);
+        else sk_cur = __ldg(&sky[pix]);
+    }
+    __device__ __forceinline__ void consume(int buf, int lane, float c2, float s2)
+    {
+        const float4* d = stage + buf * (kStageRows * 32) + lane;
+        F8 Bv;
+        Bv.a = d[0];
+        Bv.b = d[32];
+        float4 Sv;
+        if constexpr (kStageRows == 3) Sv = d[64];
+        else Sv = sk_prev;
+        pair(0, Sv, Bv, 0, c2, s2);
+    }
+    __device__ __forceinline__ void advance()
+    {
+        if constexpr (kStageRows == 2) sk_prev = sk_cur;
     }
 };
 
