@@ -432,6 +432,21 @@ __device__ __forceinline__ float asin_slope(float a, float b, float c2)
     return fmaf(c2 * c2 * 0.075f, s4, fmaf(c2 * (1.0f / 6.0f), s2, 1.0f));
 }
 
+#ifndef PISCO_BIL_FASTDIV
+#define PISCO_BIL_FASTDIV 1
+#endif
+// a / b for the stencil weights (b > 0, never an index decision): the MUFU
+// reciprocal instead of the IEEE division (c2 bilinear forward: 313.3 ms
+// against 332.0 ms; the weights move by about an ulp)
+__device__ __forceinline__ float wdiv(float a, float b)
+{
+#if PISCO_BIL_FASTDIV
+    return a * rcp_approx(b);
+#else
+    return a / b;
+#endif
+}
+
 // The same stencil in FP32 from the pair's polar-cap coordinates on the beam
 // grid: r = nside sqrt(3 (1 - cos rho)) and sigma = (qd + tp) pi/2.  Rings of
 // the north cap: ring i holds 4i pixels from 2i(i - 1), half a pixel shifted;
@@ -477,7 +492,7 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
     float w1, w2;
     if (k == 0) {
         ring(1, p1, p2, w1, w2);
-        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
+        const float wt = wdiv(r * asin_slope(r, 0.0f, c2), asin_slope(1.0f, 0.0f, c2));
         const float f = 0.25f * (1.0f - wt);
         add((p1 + 2) & 3, f);
         add((p2 + 2) & 3, f);
@@ -485,7 +500,7 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
         add(p2, fmaf(w2, wt, f));
     } else {
         const float kf = (float)k;
-        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
+        const float wt = wdiv((r - kf) * asin_slope(r, kf, c2), asin_slope(kf + 1.0f, kf, c2));
         ring(k, p1, p2, w1, w2);
         add(p1, w1 * (1.0f - wt));
         add(p2, w2 * (1.0f - wt));
@@ -494,7 +509,7 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
         add(p2, w2 * wt);
     }
     if (!(ws > 0.0f)) return false;
-    const float iw = 1.0f / ws;
+    const float iw = wdiv(1.0f, ws);
     out.a = make_float4(a.x * iw, a.y * iw, a.z * iw, a.w * iw);
     out.b = make_float4(b.x * iw, b.y * iw, b.z * iw, b.w * iw);
     return true;
@@ -525,7 +540,7 @@ __device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, flo
     };
     if (k == 0) {
         ring(1, px[2], px[3], w[2], w[3]);
-        const float wt = r * asin_slope(r, 0.0f, c2) / asin_slope(1.0f, 0.0f, c2);
+        const float wt = wdiv(r * asin_slope(r, 0.0f, c2), asin_slope(1.0f, 0.0f, c2));
         const float f = 0.25f * (1.0f - wt);
         w[0] = f;
         w[1] = f;
@@ -537,7 +552,7 @@ __device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, flo
         ring(k, px[0], px[1], w[0], w[1]);
         ring(k + 1, px[2], px[3], w[2], w[3]);
         const float kf = (float)k;
-        const float wt = (r - kf) * asin_slope(r, kf, c2) / asin_slope(kf + 1.0f, kf, c2);
+        const float wt = wdiv((r - kf) * asin_slope(r, kf, c2), asin_slope(kf + 1.0f, kf, c2));
         w[0] *= 1.0f - wt;
         w[1] *= 1.0f - wt;
         w[2] *= wt;
@@ -553,7 +568,7 @@ __device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, flo
         ws += w[i];
     }
     if (!(ws > 0.0f)) return false;
-    const float iw = 1.0f / ws;
+    const float iw = wdiv(1.0f, ws);
 #pragma unroll
     for (int i = 0; i < 4; ++i) w[i] *= iw;
     return true;
