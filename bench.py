@@ -145,6 +145,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# sample plans the TUNED forward builds per launch of its pair kernel
+PLAN_CHUNK = 1 << 22
+
 # ------------------------------------------------------------------ workload
 def max_over_ranks(value: float, dist, device) -> float:
     """The largest of every rank's value (the whole job ends with the slowest
@@ -445,9 +448,11 @@ def run_gpu_arm(args, rank, world, local):
                                        if world > 1 else "single GPU")},
             "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": n * 24,
                     "d2h_bytes_per_step": n * 8},
-            "gpu_launches": args.steps,
+            # per step: the plan kernel and the pair kernel, per 4M-sample chunk
+            "gpu_launches": args.steps * 2 * (-(-n // PLAN_CHUNK)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
+                         "kernel": "the forward step: plan_kernel + tuned_kernel",
                          "traffic": traffic,
                          "bytes_model": "48 B/pair x exact disc pairs + 32 B/sample",
                          "l2": l2_line},

@@ -141,6 +141,14 @@ pisco_status pisco_forward_device(pisco_ctx* ctx, pisco_form form, long begin, l
                                   void* d_a, void* d_b, pisco_dtype out_dtype, void* stream);
 /* Waits for the context's work and reports device-side check failures. */
 pisco_status pisco_sync(pisco_ctx* ctx);
+/* Device bytes the context holds, the figure RunConfig.maxMemUsage bounds
+ * (the reference checks its fixed buffers against it once,
+ * gpuconvolver.cu:58-70; here every buffer counts as it grows).  The TUNED
+ * forward keeps up to 4M sample plans of 96 bytes as scratch: fewer (the
+ * forward runs in chunks) when maxMemUsage leaves less room, none when it
+ * leaves room for fewer than 1024 (each warp then plans its own samples);
+ * the TOD is the same bit for bit in every case. */
+pisco_status pisco_memory_used(const pisco_ctx* ctx, size_t* bytes);
 
 /* ---- statistics of the last forward (for the roofline) ---------------- */
 /* Number of (sample, disc pixel) pairs of the current scan and the number of

@@ -120,6 +120,7 @@ SIGNATURES = [
     ("pisco_forward", _S, [_P, ctypes.c_char, _P, _P, _I, _I]),
     ("pisco_forward_device", _S, [_P, _I, _L, _L, _P, _P, _I, _P]),
     ("pisco_sync", _S, [_P]),
+    ("pisco_memory_used", _S, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     ("pisco_count_pairs", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_last_fallbacks", _S, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("pisco_tuned_calibrate", _S, [_P, _L, _L, ctypes.POINTER(ctypes.c_double),

@@ -335,6 +335,12 @@ class GPUConvolver:
     def sync(self) -> None:
         check(load().pisco_sync(self.ctx), self.ctx, "sync")
 
+    def memory_used(self) -> int:
+        """Device bytes the context holds (what RunConfig.maxMemUsage bounds)."""
+        v = ctypes.c_size_t()
+        check(load().pisco_memory_used(self.ctx, ctypes.byref(v)), self.ctx, "memory_used")
+        return int(v.value)
+
     def set_scan_device(self, n: int, d_ra: int, d_dec: int, d_pa: int, stream: int = 0) -> None:
         self._n = int(n)
         check(load().pisco_set_scan_device(self.ctx, int(n), d_ra, d_dec, d_pa, stream or None),

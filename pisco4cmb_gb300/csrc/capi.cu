@@ -66,11 +66,12 @@ pisco_ctx::~pisco_ctx()
                     (void*)adj_beam32, (void*)adj_sky_fx, (void*)adj_beam_fx, (void*)red,
                     (void*)adj_ptab, (void*)adj_ppart,
                     (void*)rings, (void*)ord, (void*)ord_keys, (void*)ord_keys2,
-                    (void*)ord_pos, ord_tmp, (void*)beam_scr})
+                    (void*)ord_pos, ord_tmp, (void*)beam_scr, plans})
         if (p) cudaFree(p);
     for (int* p : det_ord)
         if (p) cudaFree(p);
     if (ord_event) cudaEventDestroy(ord_event);
+    if (plan_event) cudaEventDestroy(plan_event);
     if (batch_event) cudaEventDestroy(batch_event);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (stream) cudaStreamDestroy(stream);
@@ -159,6 +160,53 @@ pisco_status pisco_ctx::range_order(long long begin, long long n, cudaStream_t s
 void pisco_ctx::order_used(cudaStream_t s)
 {
     if (ord_event) cudaEventRecord(ord_event, s);
+}
+
+// Sample plans built by the plan kernel (1) or by each warp (0).
+#ifndef PISCO_FWD_PLANS
+#define PISCO_FWD_PLANS 1
+#endif
+// At most 4M sample plans (384 MB of scratch); fewer when maxMemUsage leaves
+// less room (the forward then runs in chunks), none below kMinPlans.
+constexpr long long kPlanChunk = 1LL << 22;
+constexpr long long kMinPlans = 1024;
+
+void pisco_ctx::plan_scratch(long long n, cudaStream_t s, void** p, long long* cap)
+{
+    *p = nullptr;
+    *cap = 0;
+    const long long want = std::min(n, kPlanChunk);
+    long long fit = want;
+    if (cfg.maxMemUsage) {
+        const size_t room = (cfg.maxMemUsage > mem_used ? cfg.maxMemUsage - mem_used : 0) + plans_cap;
+        fit = std::min<long long>(want, (long long)(room / pisco::kSamplePlanBytes));
+    }
+    const long long need = std::min(n, kMinPlans);
+    if (fit >= need && plans_cap < pisco::kSamplePlanBytes * (size_t)fit) {
+        const std::string keep = error;
+        if (ensure(&plans, &plans_cap, pisco::kSamplePlanBytes * (size_t)fit, "sample plans") !=
+            PISCO_OK)
+            error = keep;
+    }
+    const long long have = plans ? (long long)(plans_cap / pisco::kSamplePlanBytes) : 0;
+    if (have < need) return;
+    if (!plan_event) {
+        if (cudaEventCreateWithFlags(&plan_event, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            plan_event = nullptr;
+            return;
+        }
+    } else if (cudaStreamWaitEvent(s, plan_event, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    *p = plans;
+    *cap = std::min(have, want);
+}
+
+void pisco_ctx::plans_used(cudaStream_t s)
+{
+    if (plan_event) cudaEventRecord(plan_event, s);
 }
 
 pisco_status pisco_ctx::check_device()
@@ -589,7 +637,13 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
     } else if (form == PISCO_FORM_TUNED &&
                tuned_supported(c->nside_beam, (int)c->npix_beam, c->rho_max)) {
         CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
-        e = launch_forward_tuned(a, c->sm_count, s);
+        void* plans = nullptr;
+        long long plan_cap = 0;
+#if PISCO_FWD_PLANS
+        c->plan_scratch(n, s, &plans, &plan_cap);
+#endif
+        e = launch_forward_tuned(a, c->sm_count, s, plans, plan_cap);
+        if (plans) c->plans_used(s);
     } else {
         // PLAIN, and TUNED outside the tuned geometry's domain (a beam
         // reaching beyond the polar cap of its grid).
@@ -604,6 +658,13 @@ pisco_status pisco_forward_device(pisco_ctx* c, pisco_form form, long begin, lon
         cudaStreamWaitEvent(c->stream, ev, 0);
         cudaEventDestroy(ev);
     }
+    return PISCO_OK;
+}
+
+pisco_status pisco_memory_used(const pisco_ctx* c, size_t* bytes)
+{
+    if (!c || !bytes) return PISCO_ERR_INVALID_ARGUMENT;
+    *bytes = c->mem_used;
     return PISCO_OK;
 }
 

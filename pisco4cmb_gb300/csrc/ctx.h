@@ -73,6 +73,12 @@ struct pisco_ctx {
     std::vector<size_t> det_ord_cap;
     cudaEvent_t batch_event = nullptr;  // recorded after the last batched launch
 
+    // per-sample plans of the TUNED forward (scratch of the plan kernel) and
+    // the event recorded after their last use
+    void* plans = nullptr;
+    size_t plans_cap = 0;
+    cudaEvent_t plan_event = nullptr;
+
     // staging and bookkeeping
     void* out_dev = nullptr;
     size_t out_cap = 0;
@@ -137,5 +143,12 @@ struct pisco_ctx {
     // buffer; a launch that reads it calls order_used(s) afterwards.
     pisco_status range_order(long long begin, long long n, cudaStream_t s, const int** out);
     void order_used(cudaStream_t s);
+    // Scratch for the TUNED forward's sample plans, for up to n samples (at
+    // most kPlanChunk at a time), ordered after their last use on stream s;
+    // *p = null when it does not fit within maxMemUsage or the device (the
+    // warps then build their own plans).  A launch that reads them calls
+    // plans_used(s) afterwards.
+    void plan_scratch(long long n, cudaStream_t s, void** p, long long* cap);
+    void plans_used(cudaStream_t s);
     pisco_status check_device();
 };

@@ -32,9 +32,12 @@ namespace {
 
 // kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
 // kTW: warps per block (16 / kTW blocks per SM).
-template <bool kCalib, bool kBil, int kTW>
+// Positions [pos0, pos1) of the launch.  kPlanned: plans holds their sample
+// plans (index position - pos0); otherwise each warp builds its own.
+template <bool kCalib, bool kBil, int kTW, bool kPlanned>
 __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
-    tuned_kernel(FwdArgs a, float* calib)
+    tuned_kernel(FwdArgs a, float* calib, const tuned::SamplePlan* __restrict__ plans,
+                 long long pos0, long long pos1)
 {
     // the nearest lookup stages its sky and beam reads (tuned::StagedGather)
     constexpr bool kStage = !kBil && !kCalib && PISCO_STAGE != 0;
@@ -53,12 +56,17 @@ __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
     g.sky = a.sky32;
     if constexpr (kStage) g.stage = stg + (threadIdx.x >> 5) * tuned::kStageF4;
     tuned::Queue Q{0, 0};
-    for (long long i = gw; i < a.n; i += nw) {
+    for (long long i = pos0 + gw; i < pos1; i += nw) {
         const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i
         const long long s = a.begin + j;
         const tuned::Out o{a.out_a, a.out_b, j, a.out_f64};
-        tuned::sample<kCalib, kBil>(hs, a.rings, hb, B, a.ra[s], a.dec[s], a.pa[s], o, S, Q, lane,
-                                    a.err, g, nfall, cmax, npairs);
+        const double ra = a.ra[s], dec = a.dec[s], pa = a.pa[s];
+        if constexpr (kPlanned)
+            tuned::sample_planned<kCalib, kBil>(plans[i - pos0], hs, a.rings, hb, B, ra, dec, pa, o,
+                                                S, Q, lane, a.err, g, nfall, cmax, npairs);
+        else
+            tuned::sample<kCalib, kBil>(hs, a.rings, hb, B, ra, dec, pa, o, S, Q, lane, a.err, g,
+                                        nfall, cmax, npairs);
     }
     tuned::flush<kBil>(hs, S, Q, lane, a.err, g);
     if (lane == 0 && nfall && a.fallbacks) atomicAdd(a.fallbacks, nfall);
@@ -71,6 +79,21 @@ __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
         }
     }
 }
+
+// The sample plans of positions [pos0, pos1), one thread per sample.
+__global__ void plan_kernel(FwdArgs a, tuned::SamplePlan* __restrict__ plans, long long pos0,
+                            long long pos1)
+{
+    const Hpx hs = hpx_make(a.nside_sky);
+    const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    for (long long i = pos0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < pos1;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long j = a.order ? (long long)a.order[i] : i;
+        const long long s = a.begin + j;
+        plans[i - pos0] = tuned::make_plan(hs, B, a.ra[s], a.dec[s], a.pa[s]);
+    }
+}
+static_assert(sizeof(tuned::SamplePlan) == kSamplePlanBytes, "sample plan size");
 
 __global__ void ring_table_kernel(int nside, RingT* rings)
 {
@@ -106,23 +129,42 @@ int resident_blocks(K kernel, int threads)
     return nb;
 }
 
-template <bool kCalib, bool kBil, int kTW>
-void launch_shape(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib)
+template <bool kCalib, bool kBil, int kTW, bool kPlanned>
+void launch_shape(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib,
+                  tuned::SamplePlan* plans, long long plan_cap)
 {
     const int threads = kTW * 32;
-    const long long need = (a.n + kTW - 1) / kTW;
-    const long long blocks =
-        (long long)sm_count * resident_blocks(tuned_kernel<kCalib, kBil, kTW>, threads);
-    tuned_kernel<kCalib, kBil, kTW><<<(int)(blocks < need ? blocks : need), threads, 0, st>>>(a, calib);
+    const long long resident =
+        (long long)sm_count * resident_blocks(tuned_kernel<kCalib, kBil, kTW, kPlanned>, threads);
+    const long long step = kPlanned ? plan_cap : a.n;
+    for (long long p0 = 0; p0 < a.n; p0 += step) {
+        const long long p1 = p0 + step < a.n ? p0 + step : a.n;
+        if (kPlanned) {
+            const long long pb = (p1 - p0 + 255) / 256;
+            plan_kernel<<<(int)(pb < 65536 ? pb : 65536), 256, 0, st>>>(a, plans, p0, p1);
+        }
+        const long long need = (p1 - p0 + kTW - 1) / kTW;
+        tuned_kernel<kCalib, kBil, kTW, kPlanned>
+            <<<(int)(resident < need ? resident : need), threads, 0, st>>>(a, calib, plans, p0, p1);
+    }
 }
 
-cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib)
+template <bool kBil, int kTW>
+void launch_lookup(const FwdArgs& a, int sm_count, cudaStream_t st, tuned::SamplePlan* plans,
+                   long long plan_cap)
+{
+    if (plans && plan_cap > 0) launch_shape<false, kBil, kTW, true>(a, sm_count, st, nullptr, plans, plan_cap);
+    else launch_shape<false, kBil, kTW, false>(a, sm_count, st, nullptr, nullptr, 0);
+}
+
+cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib,
+                              tuned::SamplePlan* plans, long long plan_cap)
 {
     if (a.n <= 0) return cudaSuccess;
     // calibration measures the nearest-pixel decisions, whatever the lookup
-    if (calib) launch_shape<true, false, PISCO_FWD_WARPS>(a, sm_count, st, calib);
-    else if (a.interp == 1) launch_shape<false, true, PISCO_BIL_WARPS>(a, sm_count, st, nullptr);
-    else launch_shape<false, false, PISCO_FWD_WARPS>(a, sm_count, st, nullptr);
+    if (calib) launch_shape<true, false, PISCO_FWD_WARPS, false>(a, sm_count, st, calib, nullptr, 0);
+    else if (a.interp == 1) launch_lookup<true, PISCO_BIL_WARPS>(a, sm_count, st, plans, plan_cap);
+    else launch_lookup<false, PISCO_FWD_WARPS>(a, sm_count, st, plans, plan_cap);
     return cudaGetLastError();
 }
 
@@ -147,14 +189,16 @@ cudaError_t launch_ring_table(int nside, RingT* rings, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st)
+cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st, void* plans,
+                                 long long plan_cap)
 {
-    return launch_tuned_impl(a, sm_count, st, nullptr);
+    return launch_tuned_impl(a, sm_count, st, nullptr, static_cast<tuned::SamplePlan*>(plans),
+                             plan_cap);
 }
 
 cudaError_t launch_tuned_calibrate(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib)
 {
-    return launch_tuned_impl(a, sm_count, st, calib);
+    return launch_tuned_impl(a, sm_count, st, calib, nullptr, 0);
 }
 
 }  // namespace pisco

@@ -207,9 +207,14 @@ cudaError_t launch_fixed_planes_to_float(const unsigned long long* in, void* out
 
 // PLAIN (f64 = false) and FP64 (f64 = true) forms.
 cudaError_t launch_forward_plain(const FwdArgs& a, bool f64, int sm_count, cudaStream_t st);
-// TUNED form; returns cudaErrorNotSupported when the beam does not fit the
-// north polar cap of its grid (the tuned geometry's domain).
-cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st);
+// Bytes of one sample's plan (tuned::SamplePlan, tuned_core.cuh).
+constexpr size_t kSamplePlanBytes = 96;
+// TUNED form.  plans: scratch for plan_cap sample plans (kSamplePlanBytes
+// each), or null: with it the per-sample FP64 geometry is built beforehand
+// by a kernel with one thread per sample, plan_cap samples at a time;
+// without it each warp builds its own (the same values either way).
+cudaError_t launch_forward_tuned(const FwdArgs& a, int sm_count, cudaStream_t st,
+                                 void* plans = nullptr, long long plan_cap = 0);
 bool tuned_supported(int nside_beam, int npix_beam, double rho_max);
 // Same kernel with every FP32 decision also evaluated in FP64: writes the
 // worst |FP32 - FP64| / margin seen over the non-fallback pairs to *calib.

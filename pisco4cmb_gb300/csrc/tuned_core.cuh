@@ -703,19 +703,97 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
     return swap ? 1.0f - a : a;
 }
 
-// Processes one sample.  A non-finite pointing gives NaN TOD (kSums) and no
-// pairs.  With kSums the TOD is written to `o` now, or by the drain that
-// redoes the sample's last queued pair.  nfall counts queued pairs and npairs
-// the disc pairs (lane 0 only); cmax (kCalib) is the worst FP32 decision
-// error over the non-queued pairs, in units of the margin.  kBil: bilinear
-// beam lookup (bilinear_f32; only the degenerate pairs are queued).
+// A sample's per-sample geometry: its disc (the rings it touches and the
+// edge formula's constants), the boresight frame and the psi phasors.  Built
+// by make_plan, either inside the pair kernel (one warp per sample, every
+// lane redundantly) or beforehand by plan_kernel with one thread per sample:
+// it is FP64 work (about three hundred FP64 instructions), which GB300 runs
+// at a small fraction of its FP32 rate.  96 bytes.
+struct alignas(16) SamplePlan {
+    double z0, xa, phi;       // disc: cos(theta), 1 / sin(theta), longitude (disc_plan)
+    double phi_f, dec0;       // frame: longitude reduced mod 2 pi, latitude
+    float z0f, s0f;           // frame: sin and |cos| of the latitude
+    float sps, cps, c2p, s2p; // psi phasors (negated with the frame's flip)
+    int ring_lo, ring_hi;     // rings on the edge formula
+    int full_lo, full_hi;     // rings touched
+    int flags;                // kPlanBad: non-finite pointing; kPlanAllSky
+};
+constexpr int kPlanBad = 1;
+constexpr int kPlanAllSky = 2;
+
+__device__ __forceinline__ SamplePlan make_plan(const Hpx& hs, const Beam& B, double ra,
+                                                double dec, double pa)
+{
+    SamplePlan sp;
+    const double psi = -pa;
+    if (!(isfinite(ra) && isfinite(dec) && isfinite(psi))) {
+        sp.flags = kPlanBad;
+        sp.full_lo = 1;
+        sp.full_hi = 0;
+        return sp;
+    }
+    const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, dec), ra, B.rho_max, B.cosr);
+    // Boresight frame.  The reference chain (sphtrigo.cpp:29-35) takes dec as
+    // given; for cos(dec) < 0 the same point is (pi - dec, ra + pi), and the
+    // chain's north direction then points the other way: its alpha is the
+    // normalised frame's + pi, hence its sigma is - pi, while beta and
+    // exp(2i chi) are unchanged.  So the geometry runs in the normalised frame
+    // (s0 >= 0) with (sin psi, cos psi) negated, which adds exactly pi to
+    // sigma.  ra is reduced mod 2pi (the anchor longitude of the rings).
+    // The frame is disc_plan's (z0 = cos(theta), s0, phi, latitude
+    // pi/2 - theta) whenever its reflection agrees with the sign of cos(dec),
+    // which decides the flip as in the reference chain; they can differ
+    // only within an ulp of the poles, where the frame is rebuilt from dec.
+    const bool flip = fabs(dec) < 1.5707963 ? false : cos(dec) < 0.0;
+    double z0d, s0d;
+    if (flip == P.flip) {
+        z0d = P.z0;
+        s0d = P.s0;
+        sp.phi_f = P.phi;
+        sp.dec0 = PD_SUB(kHalfPi, P.theta);
+    } else {
+        double sdec, cdec;
+        sincos(dec, &sdec, &cdec);
+        z0d = sdec;
+        s0d = fabs(cdec);
+        sp.phi_f = fmodulo(flip ? ra + kPi : ra, kTwoPi);
+        sp.dec0 = atan2(z0d, s0d);
+    }
+    sp.z0f = (float)z0d;
+    sp.s0f = (float)s0d;
+    // psi phasors in FP64, rounded once: exp(2i psi) multiplies every pair
+    // of the sample, so its rounding error is coherent over the sample sum.
+    double spsi, cpsi;
+    sincos(psi, &spsi, &cpsi);
+    sp.sps = (float)(flip ? -spsi : spsi);
+    sp.cps = (float)(flip ? -cpsi : cpsi);
+    sp.c2p = (float)__fma_rn(cpsi, cpsi, -__dmul_rn(spsi, spsi));
+    sp.s2p = (float)__dmul_rn(__dmul_rn(2.0, spsi), cpsi);
+    sp.z0 = P.z0;
+    sp.xa = P.xa;
+    sp.phi = P.phi;
+    sp.ring_lo = (int)P.ring_lo;
+    sp.ring_hi = (int)P.ring_hi;
+    sp.full_lo = (int)P.full_lo;
+    sp.full_hi = (int)P.full_hi;
+    sp.flags = P.all_sky ? kPlanAllSky : 0;
+    return sp;
+}
+
+// Processes one sample from its plan.  A non-finite pointing gives NaN TOD
+// (kSums) and no pairs.  With kSums the TOD is written to `o` now, or by the
+// drain that redoes the sample's last queued pair.  nfall counts queued pairs
+// and npairs the disc pairs (lane 0 only); cmax (kCalib) is the worst FP32
+// decision error over the non-queued pairs, in units of the margin.  kBil:
+// bilinear beam lookup (bilinear_f32; only the degenerate pairs are queued).
 template <bool kCalib, bool kBil = false, class Action>
-__device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const Hpx& hb,
-                                       const Beam& B, double ra,
-                                       double dec, double pa, const Out& o, WarpSmem& S,
-                                       Queue& Qs, int lane, unsigned int* err, Action& act,
-                                       unsigned long long& nfall, float& cmax,
-                                       unsigned long long& npairs)
+__device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& hs,
+                                               const RingT* rings, const Hpx& hb, const Beam& B,
+                                               double ra, double dec, double pa, const Out& o,
+                                               WarpSmem& S, Queue& Qs, int lane,
+                                               unsigned int* err, Action& act,
+                                               unsigned long long& nfall, float& cmax,
+                                               unsigned long long& npairs)
 {
     constexpr bool kStaged = HasStage<Action>::value && !kBil && !kCalib;
     RingC* W = S.r;
@@ -724,7 +802,7 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
     F.ra = ra;
     F.dec = dec;
     F.psi = -pa;
-    if (!(isfinite(F.ra) && isfinite(F.dec) && isfinite(F.psi))) {
+    if (SP.flags & kPlanBad) {
         if (Action::kSums && lane == 0) {
             store_out(o.a, o.f64, o.idx, CUDART_NAN);
             store_out(o.b, o.f64, o.idx, CUDART_NAN);
@@ -755,43 +833,23 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
     }
     __syncwarp();
     if constexpr (Action::kSums) act.reset();
-    const DiscPlan P = disc_plan(hs, PD_SUB(kHalfPi, F.dec), F.ra, B.rho_max, B.cosr);
-    // Boresight frame.  The reference chain (sphtrigo.cpp:29-35) takes dec as
-    // given; for cos(dec) < 0 the same point is (pi - dec, ra + pi), and the
-    // chain's north direction then points the other way: its alpha is the
-    // normalised frame's + pi, hence its sigma is - pi, while beta and
-    // exp(2i chi) are unchanged.  So the geometry runs in the normalised frame
-    // (s0 >= 0) with (sin psi, cos psi) negated, which adds exactly pi to
-    // sigma.  ra is reduced mod 2pi (the anchor longitude of the rings).
-    // The frame is disc_plan's (z0 = cos(theta), s0, phi, latitude
-    // pi/2 - theta) whenever its reflection agrees with the sign of cos(dec),
-    // which decides the flip as in the reference chain; they can differ
-    // only within an ulp of the poles, where the frame is rebuilt from dec.
-    const bool flip = fabs(F.dec) < 1.5707963 ? false : cos(F.dec) < 0.0;
-    double z0d, s0d, phi_f, dec0;
-    if (flip == P.flip) {
-        z0d = P.z0;
-        s0d = P.s0;
-        phi_f = P.phi;
-        dec0 = PD_SUB(kHalfPi, P.theta);
-    } else {
-        double sdec, cdec;
-        sincos(F.dec, &sdec, &cdec);
-        z0d = sdec;
-        s0d = fabs(cdec);
-        phi_f = fmodulo(flip ? F.ra + kPi : F.ra, kTwoPi);
-        dec0 = atan2(z0d, s0d);
-    }
-    const float z0f = (float)z0d, s0f = (float)s0d;
-    // psi phasors in FP64, rounded once: exp(2i psi) multiplies every pair
-    // of the sample, so its rounding error is coherent over the sample sum.
-    double spsi, cpsi;
-    sincos(F.psi, &spsi, &cpsi);
+    DiscPlan P;
+    P.z0 = SP.z0;
+    P.xa = SP.xa;
+    P.cosr = B.cosr;
+    P.phi = SP.phi;
+    P.ring_lo = SP.ring_lo;
+    P.ring_hi = SP.ring_hi;
+    P.full_lo = SP.full_lo;
+    P.full_hi = SP.full_hi;
+    P.all_sky = (SP.flags & kPlanAllSky) != 0;
+    const double phi_f = SP.phi_f, dec0 = SP.dec0;
+    const float z0f = SP.z0f, s0f = SP.s0f;
     F.s0 = s0f;
-    F.sps = (float)(flip ? -spsi : spsi);
-    F.cps = (float)(flip ? -cpsi : cpsi);
-    F.c2p = (float)(cpsi * cpsi - spsi * spsi);
-    F.s2p = (float)(2.0 * spsi * cpsi);
+    F.sps = SP.sps;
+    F.cps = SP.cps;
+    F.c2p = SP.c2p;
+    F.s2p = SP.s2p;
 
     for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
         const long long ring = r0 + lane;
@@ -1033,6 +1091,18 @@ __device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const 
         S.p[slot].open = 0;
     }
     __syncwarp();
+}
+
+// Processes one sample, its plan built here by the warp.
+template <bool kCalib, bool kBil = false, class Action>
+__device__ __forceinline__ void sample(const Hpx& hs, const RingT* rings, const Hpx& hb,
+                                       const Beam& B, double ra, double dec, double pa,
+                                       const Out& o, WarpSmem& S, Queue& Qs, int lane,
+                                       unsigned int* err, Action& act, unsigned long long& nfall,
+                                       float& cmax, unsigned long long& npairs)
+{
+    sample_planned<kCalib, kBil>(make_plan(hs, B, ra, dec, pa), hs, rings, hb, B, ra, dec, pa, o,
+                                 S, Qs, lane, err, act, nfall, cmax, npairs);
 }
 
 // Forward action: gather the sky, multiply by the beam, compensated sums.

@@ -1,0 +1,102 @@
+"""Sample plans of the TUNED forward (GPU).
+
+The TUNED forward builds each sample's FP64 geometry (its disc's rings and
+edge constants, the boresight frame, the psi phasors) either in a separate
+kernel with one thread per sample, into scratch the context keeps, or in
+the pair kernel's own warp.  The scratch counts against
+RunConfig.maxMemUsage (gpuconvolver.cu:58-70 is the reference's check of
+its buffers against it): with room for fewer plans than samples the
+forward runs in chunks, with room for fewer than 1024 plans the warps plan
+their own samples.  All three give the same TOD bit for bit, for both beam
+lookups, with non-finite pointings and pole pointings in the scan, and the
+scratch never takes the context beyond maxMemUsage.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PLAN_BYTES = 96
+
+
+def _setup(conv, nss=128, n=20000, seed=11):
+    import torch
+
+    from pisco4cmb_gb300 import PolBeam, Sky, beam_npix_for_radius
+
+    rng = np.random.default_rng(seed)
+    sky = rng.normal(size=(3, 12 * nss * nss)).astype(np.float32)
+    nsb = 512
+    beam = PolBeam(nsb, beam_npix_for_radius(nsb, np.deg2rad(2.5)), 0.01, "p")
+    beam.make_unpol_gaussian_elliptical_beams(1.1, 0.9, 20.0)
+    beam.build(nss)
+    ra = rng.uniform(0, 2 * np.pi, n)
+    dec = np.arcsin(rng.uniform(-1, 1, n))
+    pa = rng.uniform(0, np.pi, n)
+    dec[:6] = [np.pi / 2, -np.pi / 2, np.pi / 2 - 1e-9, -np.pi / 2 + 3e-4, 0.0, 1.2]
+    dec[7], ra[8], pa[9] = np.nan, np.inf, np.nan
+    conv.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    conv.update_beam(beam)
+    t = [torch.tensor(v, device="cuda") for v in (ra, dec, pa)]
+    conv.set_scan_device(n, *[v.data_ptr() for v in t])
+    conv._test_scan = t
+    return n
+
+
+def _tod(conv, n, interp):
+    import torch
+
+    conv.set_interp(interp)
+    a = torch.empty(n, dtype=torch.float64, device="cuda")
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    conv.forward_device(a.data_ptr(), b.data_ptr(), out_f64=True)
+    conv.sync()
+    return a.cpu().numpy(), b.cpu().numpy()
+
+
+@pytest.mark.parametrize("interp", [False, True])
+def test_planned_chunked_and_unplanned_forward_agree(gpu, interp):
+    from pisco4cmb_gb300 import GPUConvolver, RunConfig
+
+    free = GPUConvolver(form="tuned")
+    n = _setup(free)
+    before = free.memory_used()
+    ra_, rb_ = _tod(free, n, interp)
+    # one chunk: the whole scan's plans were allocated
+    assert free.memory_used() - before == PLAN_BYTES * n
+    free.close()
+    assert np.isnan(ra_[7]) and np.isnan(ra_[8]) and np.isnan(rb_[9])
+    assert np.isfinite(np.delete(ra_, [7, 8, 9])).all()
+
+    for room, chunks in ((6000, 4), (20000, 1), (1000, 0)):
+        conv = GPUConvolver(RunConfig(maxMemUsage=before + PLAN_BYTES * room, ptgPerConv=4096),
+                            form="tuned")
+        _setup(conv)
+        assert conv.memory_used() == before
+        a, b = _tod(conv, n, interp)
+        used = conv.memory_used()
+        conv.close()
+        # scratch for min(room, n) plans, none below 1024 plans of room
+        assert used - before == (PLAN_BYTES * min(room, n) if chunks else 0), (room, used - before)
+        assert np.array_equal(a, ra_, equal_nan=True), (room, np.nanmax(np.abs(a - ra_)))
+        assert np.array_equal(b, rb_, equal_nan=True), room
+
+
+def test_short_scans_and_sub_ranges_use_the_same_plans(gpu):
+    """Fewer samples than the minimum plan count, and sub-ranges of the scan
+    (begin > 0), give the full forward's TOD."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver
+
+    conv = GPUConvolver(form="tuned")
+    n = _setup(conv, n=3000, seed=5)
+    ra_, rb_ = _tod(conv, n, False)
+    for begin, m in ((0, 500), (1234, 77), (2999, 1)):
+        a = torch.empty(m, dtype=torch.float64, device="cuda")
+        b = torch.empty(m, dtype=torch.float64, device="cuda")
+        conv.forward_device(a.data_ptr(), b.data_ptr(), out_f64=True, begin=begin, n=m)
+        conv.sync()
+        assert np.array_equal(a.cpu().numpy(), ra_[begin:begin + m], equal_nan=True)
+        assert np.array_equal(b.cpu().numpy(), rb_[begin:begin + m], equal_nan=True)
+    conv.close()
