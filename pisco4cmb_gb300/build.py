@@ -21,7 +21,7 @@ LIB_NAME = "libpisco_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
 
 SOURCES = ["capi.cu", "capi_batched.cu", "capi_adjoint.cu", "fwd_plain.cu", "fwd_tuned.cu",
-           "fwd_batched.cu", "adjoint.cu", "noalloc.cu", "order.cu", "skymap.cu",
+           "fwd_batched.cu", "adjoint.cu", "adjoint_planned.cu", "noalloc.cu", "order.cu", "skymap.cu",
            "beam_dev.cu", "debug.cu", "pointing.cu", "beam_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

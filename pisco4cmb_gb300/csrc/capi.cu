@@ -166,16 +166,17 @@ void pisco_ctx::order_used(cudaStream_t s)
 #ifndef PISCO_FWD_PLANS
 #define PISCO_FWD_PLANS 1
 #endif
-// At most 4M sample plans (384 MB of scratch); fewer when maxMemUsage leaves
-// less room (the forward then runs in chunks), none below kMinPlans.
-constexpr long long kPlanChunk = 1LL << 22;
+// At most max_plans sample plans (4M: 384 MB of scratch, for the forward's
+// chunks); fewer when maxMemUsage leaves less room (the forward then runs in
+// more chunks), none below kMinPlans.
 constexpr long long kMinPlans = 1024;
 
-void pisco_ctx::plan_scratch(long long n, cudaStream_t s, void** p, long long* cap)
+void pisco_ctx::plan_scratch(long long n, cudaStream_t s, void** p, long long* cap,
+                             long long max_plans)
 {
     *p = nullptr;
     *cap = 0;
-    const long long want = std::min(n, kPlanChunk);
+    const long long want = std::min(n, max_plans);
     long long fit = want;
     if (cfg.maxMemUsage) {
         const size_t room = (cfg.maxMemUsage > mem_used ? cfg.maxMemUsage - mem_used : 0) + plans_cap;

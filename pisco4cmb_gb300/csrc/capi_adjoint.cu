@@ -182,6 +182,10 @@ pisco_status pisco_adjoint_gaussian_device(pisco_ctx* c, long begin, long n, con
 
 namespace {
 
+// Sample plans of one adjoint launch: up to 16M (1.5 GB of scratch); a
+// longer range plans in its warps.
+constexpr long long kAdjointPlans = 1LL << 24;
+
 pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, const void* d_gb,
                           pisco_dtype g_dtype, void* d_gsky, void* d_gbeam, pisco_dtype out_dtype,
                           pisco_adjoint_mode mode, cudaStream_t s, const ParamPlan* pp)
@@ -232,6 +236,12 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
         a.ceps_i = pp->ci;
         a.ceps_q = pp->cq;
     }
+    // the samples' plans, if the whole range fits the scratch (the launch is
+    // not split: the parameter gradient's per-warp rows cover one launch)
+    void* plans = nullptr;
+    long long plan_cap = 0;
+    if (n > 0) c->plan_scratch(n, s, &plans, &plan_cap, kAdjointPlans);
+    if (plan_cap >= n) a.plans = static_cast<tuned::SamplePlan*>(plans);
     int nwarps = 0;
     CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
     if (!deterministic) {
@@ -260,6 +270,7 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
         a.gbeam32 = gbm;
         if (n > 0) CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
+        if (a.plans) c->plans_used(s);
         if (d_gsky && out_dtype == PISCO_FLOAT64) {
             widen_f32<<<1024, 256, 0, s>>>(gs, (double*)d_gsky, nsky);
             CK(cudaGetLastError(), "widen sky gradient");
@@ -308,6 +319,7 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
         if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0 || pp))
             CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
+        if (a.plans) c->plans_used(s);
         if (d_gsky)
             CK(launch_fixed_planes_to_float(c->adj_sky_fx, d_gsky, out_dtype == PISCO_FLOAT64, npix,
                                             a.sky_scale > 0.0 ? 1.0 / a.sky_scale : 0.0, s),

@@ -75,14 +75,18 @@ pisco_status validate(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_
 }
 
 std::string launch_key(pisco_ctx* c, const pisco_det_desc* dets, int ndet, pisco_dtype out_dtype,
-                       int chunk, int warps)
+                       int chunk, int warps, const void* plans)
 {
     std::string k((const char*)dets, sizeof(pisco_det_desc) * (size_t)ndet);
-    char tail[128];
-    std::snprintf(tail, sizeof tail, "|%d|%d|%d|%p|%d|%d", chunk, warps, (int)out_dtype,
-                  (void*)c->sky32, c->nside_sky, (int)c->interp);
+    char tail[160];
+    std::snprintf(tail, sizeof tail, "|%d|%d|%d|%p|%d|%d|%p", chunk, warps, (int)out_dtype,
+                  (void*)c->sky32, c->nside_sky, (int)c->interp, plans);
     return k + tail;
 }
+
+// Sample plans of a batched launch: all its detectors' samples at once, up
+// to 16M (1.5 GB of scratch); a larger launch plans in its warps.
+constexpr long long kBatchPlans = 1LL << 24;
 
 // One autotuned choice: chunk, warps per block, time.
 struct Tuned {
@@ -186,7 +190,15 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
     st = c->activate();
     if (st != PISCO_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
-    const std::string key = launch_key(c, dets, ndet, out_dtype, chunk, warps);
+    // every detector's sample plans in one scratch (planned launch), if it
+    // fits: the graph below holds its address
+    long long total = 0;
+    for (int d = 0; d < ndet; ++d) total += dets[d].nsamples;
+    void* plans = nullptr;
+    long long plan_cap = 0;
+    if (total > 0) c->plan_scratch(total, s, &plans, &plan_cap, kBatchPlans);
+    if (plan_cap < total) plans = nullptr;
+    const std::string key = launch_key(c, dets, ndet, out_dtype, chunk, warps, plans);
     if (!(c->graph_exec && key == c->graph_key)) {
         // the descriptors, items and orders below may still be read by the
         // previous launch (on another stream)
@@ -212,6 +224,11 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
                              dets[d].ra, dets[d].dec, dets[d].pa, dets[d].tod_a, dets[d].tod_b,
                              order};
             cost[d] = disc_pairs(c->nside_sky, sl.rho_max);
+        }
+        long long base = 0;
+        for (int d = 0; d < ndet; ++d) {
+            bd[d].plan_base = base;
+            base += dets[d].nsamples;
         }
         const std::vector<BatchItem> items = make_items(bd, cost, chunk);
         if (items.size() > (size_t)0x7fffffff) return fail(c, PISCO_ERR_INVALID_ARGUMENT, "too many queue items");
@@ -242,7 +259,9 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         a.err = c->d_err;
         a.fallbacks = c->d_fallbacks;
         a.interp = (int)c->interp;
-        // capture (queue reset + kernel) once; replays reuse it
+        a.plans = static_cast<tuned::SamplePlan*>(plans);
+        a.nplans = plans ? total : 0;
+        // capture (queue reset + plan kernel + kernel) once; replays reuse it
         if (c->graph_exec) {
             cudaGraphExecDestroy(c->graph_exec);
             c->graph_exec = nullptr;
@@ -268,6 +287,7 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         c->graph_key = key;
     }
     CK(cudaGraphLaunch(c->graph_exec, s), "graph launch");
+    if (plans) c->plans_used(s);
     if (!c->batch_event) CK(cudaEventCreateWithFlags(&c->batch_event, cudaEventDisableTiming), "event");
     CK(cudaEventRecord(c->batch_event, s), "batch event");
     return PISCO_OK;

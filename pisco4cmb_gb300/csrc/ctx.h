@@ -148,7 +148,8 @@ struct pisco_ctx {
     // *p = null when it does not fit within maxMemUsage or the device (the
     // warps then build their own plans).  A launch that reads them calls
     // plans_used(s) afterwards.
-    void plan_scratch(long long n, cudaStream_t s, void** p, long long* cap);
+    void plan_scratch(long long n, cudaStream_t s, void** p, long long* cap,
+                      long long max_plans = 1LL << 22);
     void plans_used(cudaStream_t s);
     pisco_status check_device();
 };

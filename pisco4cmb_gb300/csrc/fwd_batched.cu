@@ -8,8 +8,9 @@
 // samples into chunks, orders the chunks longest-first (estimated pairs),
 // and one kernel whose blocks pull chunks with one atomic each runs them all
 // (the warps of a block share a chunk, sample by sample).
-// The launch (queue reset + kernel) is captured once in a CUDA graph and
-// replayed while the same detector set is resubmitted.  The chunk size and
+// The launch (queue reset, the plan kernel that builds every sample's FP64
+// geometry with one thread per sample, the batched kernel) is captured once
+// in a CUDA graph and replayed while the same detector set is resubmitted.  The chunk size and
 // the block shape (warps per block) are chosen by the autotuner
 // (pisco_autotune_batched) and cached per workload key in a JSON file.
 //
@@ -50,14 +51,43 @@ struct ItemState {
     void* out_b;
     const int* order;  // position -> sample, or null
     long long begin, end;
+    long long plan_base;
     int state;  // 0: queue empty, 1: run, 2: bad item (skipped)
 };
+
+// Every detector's sample plans (position p of detector d at
+// plans[plan_base + p]; the bases ascend with d and end at a.nplans), one
+// thread per sample over all detectors at once: the FP64 per-sample geometry
+// the warps would otherwise build themselves (tuned_core.cuh make_plan).
+__global__ void batched_plan_kernel(BatchArgs a)
+{
+    const Hpx hs = hpx_make(a.nside_sky);
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < a.nplans;
+         g += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.ndet - 1;  // the last detector whose plans start at or before g
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.dets[mid].plan_base <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchDet& det = a.dets[lo];
+        const long long p = g - det.plan_base;
+        if (p < 0 || p >= det.n) {
+            tuned::record(a.err, kCheckQueue);
+            continue;
+        }
+        const tuned::Beam B = tuned::make_beam(det.beam, det.nside_beam, det.npix_beam, det.rho_max);
+        const long long s = det.order ? (long long)det.order[p] : p;
+        a.plans[g] = tuned::make_plan(hs, B, det.ra[s], det.dec[s], det.pa[s]);
+    }
+}
 
 // kBil: bilinear beam lookup (tuned_core.cuh bilinear_f32).  kW: warps per
 // block, the tile the autotuner picks with the chunk size; every shape keeps
 // 16 warps per SM (16 / kW blocks), so all compile to the same 128-register
 // cap and differ in how many warps share an item (and its samples' discs).
-template <bool kBil, int kW>
+// kPlanned: the samples' plans come from batched_plan_kernel.
+template <bool kBil, int kW, bool kPlanned>
 __global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
 {
     constexpr int kBW = kW;
@@ -94,6 +124,7 @@ __global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
                     T.out_a = d.out_a;
                     T.out_b = d.out_b;
                     T.order = d.order;
+                    T.plan_base = d.plan_base;
                     T.begin = it.begin;
                     T.end = it.begin + it.count;
                     T.state = 1;
@@ -107,8 +138,13 @@ __global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
         for (long long p = T.begin + warp; p < T.end; p += kBW) {
             const long long s = T.order ? (long long)T.order[p] : p;  // sample of position p
             const tuned::Out o{T.out_a, T.out_b, s, a.out_f64};
-            tuned::sample<false, kBil>(hs, a.rings, T.hb, T.B, T.ra[s], T.dec[s], T.pa[s], o, S,
-                                       Q, lane, a.err, g, nfall, cmax, npairs);
+            if constexpr (kPlanned)
+                tuned::sample_planned<false, kBil>(a.plans[T.plan_base + p], hs, a.rings, T.hb, T.B,
+                                                   T.ra[s], T.dec[s], T.pa[s], o, S, Q, lane, a.err,
+                                                   g, nfall, cmax, npairs);
+            else
+                tuned::sample<false, kBil>(hs, a.rings, T.hb, T.B, T.ra[s], T.dec[s], T.pa[s], o,
+                                           S, Q, lane, a.err, g, nfall, cmax, npairs);
         }
     }
     tuned::flush<kBil>(hs, S, Q, lane, a.err, g);
@@ -123,7 +159,7 @@ template <int kW>
 int grid_of(int sm_count)
 {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false, kW>, kW * 32, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false, kW, true>, kW * 32, 0) !=
             cudaSuccess ||
         nb < 1)
         nb = 1;
@@ -133,8 +169,15 @@ int grid_of(int sm_count)
 template <int kW>
 void launch_shape(const BatchArgs& a, int grid, cudaStream_t st)
 {
-    if (a.interp == 1) batched_kernel<true, kW><<<grid, kW * 32, 0, st>>>(a);
-    else batched_kernel<false, kW><<<grid, kW * 32, 0, st>>>(a);
+    if (a.plans) {
+        const long long pb = (a.nplans + 255) / 256;
+        batched_plan_kernel<<<(int)(pb < 65536 ? pb : 65536), 256, 0, st>>>(a);
+        if (a.interp == 1) batched_kernel<true, kW, true><<<grid, kW * 32, 0, st>>>(a);
+        else batched_kernel<false, kW, true><<<grid, kW * 32, 0, st>>>(a);
+    } else {
+        if (a.interp == 1) batched_kernel<true, kW, false><<<grid, kW * 32, 0, st>>>(a);
+        else batched_kernel<false, kW, false><<<grid, kW * 32, 0, st>>>(a);
+    }
 }
 
 }  // namespace

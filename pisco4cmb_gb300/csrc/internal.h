@@ -15,6 +15,10 @@
 
 namespace pisco {
 
+namespace tuned {
+struct SamplePlan;  // tuned_core.cuh
+}
+
 struct alignas(32) D4 {
     double x, y, z, w;
 };
@@ -94,6 +98,7 @@ struct BatchDet {
     void* out_a;
     void* out_b;
     const int* order;  // position -> sample (sky order) or null
+    long long plan_base;  // planned launch: its plans start at BatchArgs::plans[plan_base]
 };
 
 // One unit of the work queue: samples [begin, begin + count) of detector det.
@@ -116,6 +121,10 @@ struct BatchArgs {
     unsigned int* err;
     unsigned long long* fallbacks;
     int interp = 0;  // 0 nearest, 1 bilinear beam lookup
+    // sample plans of every detector's positions (BatchDet::plan_base), built
+    // by a plan kernel before the batched kernel; null: each warp plans its own
+    tuned::SamplePlan* plans = nullptr;
+    long long nplans = 0;  // sum of the detectors' samples
 };
 
 struct AdjArgs {
@@ -150,6 +159,9 @@ struct AdjArgs {
     const float* ptab = nullptr;
     double* ppart = nullptr;
     float ceps_i = 1.0f, ceps_q = 1.0f;
+    // the samples' plans (a.n of them, index: position), built by the planned
+    // launch itself into this scratch; null: each warp plans its own samples
+    tuned::SamplePlan* plans = nullptr;
 };
 
 // Per-pair record of a form's decisions (pisco_debug_pairs, debug.cu): the
@@ -196,6 +208,8 @@ cudaError_t launch_fold_params(const double* ppart, int nwarps, double* row, cud
 int adjoint_max_warps(int sm_count);
 // nwarps (optional): the warps of the launch's grid (the rows of ppart it writes).
 cudaError_t launch_adjoint(const AdjArgs& a, int sm_count, cudaStream_t st, int* nwarps = nullptr);
+// The same with a.plans: the plan kernel, then the planned kernels (adjoint_planned.cu).
+cudaError_t launch_adjoint_planned(const AdjArgs& a, int sm_count, cudaStream_t st, int* nwarps);
 cudaError_t launch_abs_sum(const void* ga, const void* gb, int f64, long long n, double* part,
                            cudaStream_t st);
 cudaError_t launch_abs_max(const float* x, long long n, double* part, cudaStream_t st);
