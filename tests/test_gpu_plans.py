@@ -100,3 +100,30 @@ def test_short_scans_and_sub_ranges_use_the_same_plans(gpu):
         assert np.array_equal(a.cpu().numpy(), ra_[begin:begin + m], equal_nan=True)
         assert np.array_equal(b.cpu().numpy(), rb_[begin:begin + m], equal_nan=True)
     conv.close()
+
+
+def test_forwards_on_two_streams_share_the_plan_scratch(gpu):
+    """Two forwards of one context on different streams, back to back with
+    no host synchronisation: the second waits for the first's use of the
+    plan scratch, and both give the single-stream TOD."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver
+
+    conv = GPUConvolver(form="tuned")
+    n = _setup(conv, n=40000, seed=9)
+    ref = _tod(conv, n, False)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    outs = []
+    for st, (b0, m) in ((s1, (0, n)), (s2, (n // 3, n - n // 3)), (s1, (5, 1000))):
+        a = torch.empty(m, dtype=torch.float64, device="cuda")
+        b = torch.empty(m, dtype=torch.float64, device="cuda")
+        conv.forward_device(a.data_ptr(), b.data_ptr(), out_f64=True, begin=b0, n=m,
+                            stream=st.cuda_stream)
+        outs.append((b0, m, a, b))
+    torch.cuda.synchronize()
+    conv.sync()
+    for b0, m, a, b in outs:
+        assert np.array_equal(a.cpu().numpy(), ref[0][b0:b0 + m], equal_nan=True)
+        assert np.array_equal(b.cpu().numpy(), ref[1][b0:b0 + m], equal_nan=True)
+    conv.close()
