@@ -329,18 +329,43 @@ struct HasFinish : std::false_type {};
 template <class A>
 struct HasFinish<A, std::void_t<decltype(&A::finish)>> : std::true_type {};
 
+// Warps per SM of an instance: the planned nearest lookup runs 32 (register
+// cap 64, its plan and descriptors in shared memory, as the forward does),
+// the others 16 (cap 128).  The DETERMINISTIC beam-map gradient stays at 16:
+// its action spills at 64 registers (c5: 95 ms against 87 ms).
+template <class Act, bool kBil, bool kPlanned>
+constexpr int adj_warps_per_sm()
+{
+    return kPlanned && !kBil && !std::is_same_v<Act, ScatterBeam<true>> ? 32 : 16;
+}
+
 // kBil: the transpose of the TUNED forward with the bilinear beam lookup.
 // kPlanned: a.plans holds the samples' plans (index: position), built by
 // adjoint_plan_kernel; otherwise each warp builds its own.
 template <class Act, bool kBil, bool kPlanned>
-__global__ void __launch_bounds__(kAW * 32, PISCO_TUNED_MINB) adjoint_kernel(AdjArgs a, Act proto)
+__global__ void __launch_bounds__(kAW * 32, adj_warps_per_sm<Act, kBil, kPlanned>() / kAW)
+    adjoint_kernel(AdjArgs a, Act proto)
 {
+    constexpr bool kDescSmem = adj_warps_per_sm<Act, kBil, kPlanned>() == 32;
     __shared__ tuned::WarpSmem sm[kAW];
+    __shared__ Hpx s_hs, s_hb;
+    __shared__ tuned::Beam s_B;
     const int lane = threadIdx.x & 31;
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
-    const Hpx hs = hpx_make(a.nside_sky);
-    const Hpx hb = hpx_make(a.nside_beam);
-    const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    const Hpx rhs = hpx_make(a.nside_sky);
+    const Hpx rhb = hpx_make(a.nside_beam);
+    const tuned::Beam rB = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    if constexpr (kDescSmem) {
+        if (threadIdx.x == 0) {
+            s_hs = rhs;
+            s_hb = rhb;
+            s_B = rB;
+        }
+        __syncthreads();
+    }
+    const Hpx& hs = kDescSmem ? s_hs : rhs;
+    const Hpx& hb = kDescSmem ? s_hb : rhb;
+    const tuned::Beam& B = kDescSmem ? s_B : rB;
     const long long gw = (long long)blockIdx.x * kAW + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kAW;
     unsigned long long nfall = 0, npairs = 0;

@@ -1,9 +1,11 @@
 // adjoint_planned.cu -- the adjoint's kernels reading sample plans built
 // beforehand: adjoint_plan_kernel builds each sample's FP64 geometry (its
 // disc, frame and psi phasors; tuned_core.cuh make_plan) with one thread per
-// sample, then the kernels of adjoint_kernels.cuh run with kPlanned.  The
-// plans are the values the warps would build, so the gradients are the same
-// bit for bit.
+// sample, then the kernels of adjoint_kernels.cuh run with kPlanned (the
+// nearest lookup at 32 warps per SM).  The plans are the values the warps
+// would build, so the pairs and their values are the same: the fixed-point
+// (DETERMINISTIC) sky and beam gradients are the same bit for bit, while the
+// parameter gradient's per-warp partial sums follow the launch's warps.
 #include <cuda_runtime.h>
 
 #include "adjoint_kernels.cuh"

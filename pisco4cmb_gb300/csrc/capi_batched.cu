@@ -271,7 +271,7 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned int), c->stream);
         cudaError_t e2 = e1 == cudaSuccess
-                             ? launch_batched(a, batched_grid(c->sm_count, warps), c->stream, warps)
+                             ? launch_batched(a, c->sm_count, c->stream, warps)
                              : e1;
         cudaError_t e3 = cudaStreamEndCapture(c->stream, &g);
         if (e2 != cudaSuccess || e3 != cudaSuccess) {

@@ -82,21 +82,35 @@ __global__ void batched_plan_kernel(BatchArgs a)
     }
 }
 
+// Warps per SM of an instance: the planned nearest lookup runs 32 (register
+// cap 64: its per-sample plan and the descriptors are in shared memory, as in
+// the single-detector launch), the others 16 (cap 128).
+template <bool kBil, bool kPlanned>
+constexpr int warps_per_sm()
+{
+    return kPlanned && !kBil ? 32 : 16;
+}
+
 // kBil: bilinear beam lookup (tuned_core.cuh bilinear_f32).  kW: warps per
-// block, the tile the autotuner picks with the chunk size; every shape keeps
-// 16 warps per SM (16 / kW blocks), so all compile to the same 128-register
-// cap and differ in how many warps share an item (and its samples' discs).
-// kPlanned: the samples' plans come from batched_plan_kernel.
+// block, the tile the autotuner picks with the chunk size; every tile of an
+// instance keeps the same warps per SM (warps_per_sm / kW blocks), so all
+// compile to the same register cap and differ in how many warps share an
+// item (and its samples' discs).  kPlanned: the samples' plans come from
+// batched_plan_kernel.
 template <bool kBil, int kW, bool kPlanned>
-__global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
+__global__ void __launch_bounds__(kW * 32, warps_per_sm<kBil, kPlanned>() / kW)
+    batched_kernel(BatchArgs a)
 {
     constexpr int kBW = kW;
     __shared__ tuned::WarpSmem sm[kBW];
     __shared__ ItemState s_item[2];
+    __shared__ Hpx s_hs;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     tuned::WarpSmem& S = sm[warp];
-    const Hpx hs = hpx_make(a.nside_sky);
+    if (threadIdx.x == 0) s_hs = hpx_make(a.nside_sky);
+    __syncthreads();
+    const Hpx& hs = s_hs;
     unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
     tuned::Gather g;
@@ -155,28 +169,35 @@ __global__ void __launch_bounds__(kW * 32, 16 / kW) batched_kernel(BatchArgs a)
 
 namespace {
 
-template <int kW>
+// Resident blocks of an instance on the whole GPU (its persistent grid).
+template <bool kBil, int kW, bool kPlanned>
 int grid_of(int sm_count)
 {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<false, kW, true>, kW * 32, 0) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<kBil, kW, kPlanned>, kW * 32,
+                                                      0) != cudaSuccess ||
         nb < 1)
         nb = 1;
     return sm_count * nb;
 }
 
+template <bool kBil, int kW, bool kPlanned>
+void launch_one(const BatchArgs& a, int sm_count, cudaStream_t st)
+{
+    batched_kernel<kBil, kW, kPlanned><<<grid_of<kBil, kW, kPlanned>(sm_count), kW * 32, 0, st>>>(a);
+}
+
 template <int kW>
-void launch_shape(const BatchArgs& a, int grid, cudaStream_t st)
+void launch_shape(const BatchArgs& a, int sm_count, cudaStream_t st)
 {
     if (a.plans) {
         const long long pb = (a.nplans + 255) / 256;
         batched_plan_kernel<<<(int)(pb < 65536 ? pb : 65536), 256, 0, st>>>(a);
-        if (a.interp == 1) batched_kernel<true, kW, true><<<grid, kW * 32, 0, st>>>(a);
-        else batched_kernel<false, kW, true><<<grid, kW * 32, 0, st>>>(a);
+        if (a.interp == 1) launch_one<true, kW, true>(a, sm_count, st);
+        else launch_one<false, kW, true>(a, sm_count, st);
     } else {
-        if (a.interp == 1) batched_kernel<true, kW, false><<<grid, kW * 32, 0, st>>>(a);
-        else batched_kernel<false, kW, false><<<grid, kW * 32, 0, st>>>(a);
+        if (a.interp == 1) launch_one<true, kW, false>(a, sm_count, st);
+        else launch_one<false, kW, false>(a, sm_count, st);
     }
 }
 
@@ -184,17 +205,12 @@ void launch_shape(const BatchArgs& a, int grid, cudaStream_t st)
 
 bool batched_warps_valid(int warps) { return warps == 4 || warps == 8 || warps == 16; }
 
-int batched_grid(int sm_count, int warps)
-{
-    return warps == 4 ? grid_of<4>(sm_count) : warps == 16 ? grid_of<16>(sm_count) : grid_of<8>(sm_count);
-}
-
-cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st, int warps)
+cudaError_t launch_batched(const BatchArgs& a, int sm_count, cudaStream_t st, int warps)
 {
     if (a.nitems <= 0) return cudaSuccess;
-    if (warps == 4) launch_shape<4>(a, grid, st);
-    else if (warps == 16) launch_shape<16>(a, grid, st);
-    else launch_shape<8>(a, grid, st);
+    if (warps == 4) launch_shape<4>(a, sm_count, st);
+    else if (warps == 16) launch_shape<16>(a, sm_count, st);
+    else launch_shape<8>(a, sm_count, st);
     return cudaGetLastError();
 }
 

@@ -14,28 +14,39 @@
 namespace pisco {
 namespace {
 
-// Launch shape: the nearest lookup runs one block of 16 warps per SM
-// (register cap 128, the same as 8 warps x 2 blocks): the 16 warps of an SM
-// then work on 16 consecutive samples, whose discs overlap, instead of two
-// groups of 8 far apart, so their sky reads share L1 (c2 forward: 174.8 ms
-// against 176.7 ms for 8 x 2 and 178.7 ms for 4 x 4).  Its 83 KB of per-warp
+// Launch shape: the nearest lookup runs one block of 32 warps per SM
+// (register cap 64).  The kernel is latency-bound, and with each sample's
+// plan (WarpSmem::plan) and the grids' and beam's descriptors in shared
+// memory, read where needed, its pair loop fits 64 registers with little
+// spilling, so eight warps per scheduler hide what four could not (c2
+// forward: 129.9 ms, against 169.7 ms for 16 warps at 128 registers; with
+// the descriptors in registers 20 warps gave 162.1 ms and 24 warps, spilling
+// inside the loop, 174.6 ms).  The 32 warps work on consecutive samples,
+// whose discs overlap, so their sky reads share L1.  Its 169 KB of per-warp
 // shared state is a static allocation, which sm_103a allows beyond 48 KB.
-// The bilinear lookup, whose four stencil reads per pair want L1 for
-// themselves, runs 8 x 2 (348.4 ms against 368.5 ms for 16 x 1, both with
-// one allocating 256-bit load per stencil pixel).
+// The bilinear lookup, which needs more registers per pair, runs 8 x 2 with
+// its descriptors in registers (296.3 ms; from shared memory 374.1 ms).
 #ifndef PISCO_FWD_WARPS
-#define PISCO_FWD_WARPS 16
+#define PISCO_FWD_WARPS 32
 #endif
 #ifndef PISCO_BIL_WARPS
 #define PISCO_BIL_WARPS 8
 #endif
 
 // kBil: bilinear beam lookup (the PLAIN form's get_interpol stencil in FP32).
-// kTW: warps per block (16 / kTW blocks per SM).
+// kTW: warps per block (fwd_warps_per_sm / kTW blocks per SM).
 // Positions [pos0, pos1) of the launch.  kPlanned: plans holds their sample
 // plans (index position - pos0); otherwise each warp builds its own.
+// Warps per SM: 32 for the planned nearest lookup (register cap 64), 16 for
+// the others (cap 128).
+template <bool kCalib, bool kBil, bool kPlanned>
+constexpr int fwd_warps_per_sm()
+{
+    return kPlanned && !kBil && !kCalib ? 32 : 16;
+}
+
 template <bool kCalib, bool kBil, int kTW, bool kPlanned>
-__global__ void __launch_bounds__(kTW * 32, 16 / kTW)
+__global__ void __launch_bounds__(kTW * 32, fwd_warps_per_sm<kCalib, kBil, kPlanned>() / kTW)
     tuned_kernel(FwdArgs a, float* calib, const tuned::SamplePlan* __restrict__ plans,
                  long long pos0, long long pos1)
 {
@@ -45,9 +56,28 @@ __global__ void __launch_bounds__(kTW * 32, 16 / kTW)
     __shared__ float4 stg[kStage ? kTW * tuned::kStageF4 : 1];
     const int lane = threadIdx.x & 31;
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
-    const Hpx hs = hpx_make(a.nside_sky);
-    const Hpx hb = hpx_make(a.nside_beam);
-    const tuned::Beam B = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    // The nearest lookup keeps the grids' and the beam's descriptors in
+    // shared memory, read where needed rather than held in registers across
+    // the pair loop: at its 64-register cap (32 warps per SM) that leaves the
+    // registers to the pair geometry.  The bilinear lookup, which reads the
+    // beam descriptor on every stencil pixel, keeps them in registers.
+    constexpr bool kDescSmem = !kBil;
+    __shared__ Hpx s_hs, s_hb;
+    __shared__ tuned::Beam s_B;
+    const Hpx rhs = hpx_make(a.nside_sky);
+    const Hpx rhb = hpx_make(a.nside_beam);
+    const tuned::Beam rB = tuned::make_beam(a.beam32, a.nside_beam, a.npix_beam, a.rho_max);
+    if constexpr (kDescSmem) {
+        if (threadIdx.x == 0) {
+            s_hs = rhs;
+            s_hb = rhb;
+            s_B = rB;
+        }
+        __syncthreads();
+    }
+    const Hpx& hs = kDescSmem ? s_hs : rhs;
+    const Hpx& hb = kDescSmem ? s_hb : rhb;
+    const tuned::Beam& B = kDescSmem ? s_B : rB;
     const long long gw = (long long)blockIdx.x * kTW + (threadIdx.x >> 5);
     const long long nw = (long long)gridDim.x * kTW;
     unsigned long long nfall = 0, npairs = 0;
@@ -149,12 +179,25 @@ void launch_shape(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib,
     }
 }
 
+// kTW: the planned launch's block; without plans the warps build their own
+// (FP64 disc plan in the loop's registers), which spills at 64 registers, so
+// that launch keeps 16 warps per SM.  A planned launch of fewer than four
+// samples per resident warp uses blocks of 8 warps (4 per SM), so that its
+// samples spread over every SM (32-warp blocks would fill n / 32 SMs).
 template <bool kBil, int kTW>
 void launch_lookup(const FwdArgs& a, int sm_count, cudaStream_t st, tuned::SamplePlan* plans,
                    long long plan_cap)
 {
-    if (plans && plan_cap > 0) launch_shape<false, kBil, kTW, true>(a, sm_count, st, nullptr, plans, plan_cap);
-    else launch_shape<false, kBil, kTW, false>(a, sm_count, st, nullptr, nullptr, 0);
+    constexpr int kUnplanned = kTW > 16 ? 16 : kTW;
+    if (plans && plan_cap > 0) {
+        const long long chunk = plan_cap < a.n ? plan_cap : a.n;
+        if (kTW > 8 && chunk < 4LL * sm_count * kTW)
+            launch_shape<false, kBil, (kTW > 8 ? 8 : kTW), true>(a, sm_count, st, nullptr, plans, plan_cap);
+        else
+            launch_shape<false, kBil, kTW, true>(a, sm_count, st, nullptr, plans, plan_cap);
+    } else {
+        launch_shape<false, kBil, kUnplanned, false>(a, sm_count, st, nullptr, nullptr, 0);
+    }
 }
 
 cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, float* calib,
@@ -162,7 +205,7 @@ cudaError_t launch_tuned_impl(const FwdArgs& a, int sm_count, cudaStream_t st, f
 {
     if (a.n <= 0) return cudaSuccess;
     // calibration measures the nearest-pixel decisions, whatever the lookup
-    if (calib) launch_shape<true, false, PISCO_FWD_WARPS, false>(a, sm_count, st, calib, nullptr, 0);
+    if (calib) launch_shape<true, false, 16, false>(a, sm_count, st, calib, nullptr, 0);
     else if (a.interp == 1) launch_lookup<true, PISCO_BIL_WARPS>(a, sm_count, st, plans, plan_cap);
     else launch_lookup<false, PISCO_FWD_WARPS>(a, sm_count, st, plans, plan_cap);
     return cudaGetLastError();

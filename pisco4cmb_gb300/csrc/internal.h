@@ -243,10 +243,11 @@ cudaError_t sky_order(long long n, const double* ra, const double* dec, unsigned
 // Fills the sky ring table (4 nside - 1 entries) for nside <= 8192.
 cudaError_t launch_ring_table(int nside, RingT* rings, cudaStream_t st);
 // Batched TUNED forward (fwd_batched.cu).
-// warps: warps per block, 4, 8 or 16 (16 warps per SM in every shape).
+// warps: warps per block, 4, 8 or 16 (32 warps per SM for the planned nearest
+// lookup, 16 otherwise, in every shape).
 bool batched_warps_valid(int warps);
-int batched_grid(int sm_count, int warps = 8);
-cudaError_t launch_batched(const BatchArgs& a, int grid, cudaStream_t st, int warps = 8);
+// The persistent grid is the instance's resident blocks on sm_count SMs.
+cudaError_t launch_batched(const BatchArgs& a, int sm_count, cudaStream_t st, int warps = 8);
 // Per-sample disc sizes (pairs) for the roofline byte model.
 cudaError_t launch_count_pairs(int nside_sky, double rho_max, long long n, const double* ra,
                                const double* dec, unsigned long long* total, int sm_count,

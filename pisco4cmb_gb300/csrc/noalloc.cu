@@ -213,7 +213,7 @@ extern "C" pisco_status pisco_forward_batched_noalloc(int device, int nside_sky,
     a.err = &scratch->err;
     a.fallbacks = &scratch->fallbacks;
     cudaError_t e = e0;
-    if (e == cudaSuccess) e = launch_batched(a, batched_grid(sms), st);
+    if (e == cudaSuccess) e = launch_batched(a, sms, st);
     // synchronous: read the device error word back
     unsigned int code = 0;
     if (e == cudaSuccess)

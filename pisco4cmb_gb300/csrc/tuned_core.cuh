@@ -133,9 +133,29 @@ struct alignas(16) Pend {
     int f64;                 // output type
 };
 
-// Per-warp shared state: one ring batch, the samples in flight and the FP64
-// re-evaluation queue (sky pixel, slot).
+// A sample's per-sample geometry: its disc (the rings it touches and the
+// edge formula's constants), the boresight frame and the psi phasors.  Built
+// by make_plan, either inside the pair kernel (one warp per sample, every
+// lane redundantly) or beforehand by plan_kernel with one thread per sample:
+// it is FP64 work (about three hundred FP64 instructions), which GB300 runs
+// at a small fraction of its FP32 rate.  96 bytes.
+struct alignas(16) SamplePlan {
+    double z0, xa, phi;       // disc: cos(theta), 1 / sin(theta), longitude (disc_plan)
+    double phi_f, dec0;       // frame: longitude reduced mod 2 pi, latitude
+    float z0f, s0f;           // frame: sin and |cos| of the latitude
+    float sps, cps, c2p, s2p; // psi phasors (negated with the frame's flip)
+    int ring_lo, ring_hi;     // rings on the edge formula
+    int full_lo, full_hi;     // rings touched
+    int flags;                // kPlanBad: non-finite pointing; kPlanAllSky
+};
+constexpr int kPlanBad = 1;
+constexpr int kPlanAllSky = 2;
+
+// Per-warp shared state: one ring batch, the samples in flight, the FP64
+// re-evaluation queue (sky pixel, slot) and the current sample's plan (read
+// from here where needed rather than held in registers across the pair loop).
 struct WarpSmem {
+    SamplePlan plan;
     RingC r[32];
     Pend p[kPend];
     int q[kQCap];
@@ -327,18 +347,18 @@ __device__ __forceinline__ F8 load_beam_stencil(const F8* p)
 // The disc's pixel range(s) on one ring: FP32 edge angle, FP64 positions,
 // exact FP64 HEALPix formula (disc_ring) whenever an edge decision is within
 // the FP32 angle's error of a pixel boundary.  Same result as disc_ring.
-__device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan& p, long long ring,
-                                                   const RingT& rt)
+__device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const SamplePlan& p, double cosr,
+                                                   long long ring, const RingT& rt)
 {
     RingSpan s = {0, 0, 0, 0};
     if (ring < p.full_lo || ring > p.full_hi) return s;
     const long long npix = rt.npix2 >> 1;
-    if (p.all_sky || ring < p.ring_lo || ring > p.ring_hi) {
+    if ((p.flags & kPlanAllSky) || ring < p.ring_lo || ring > p.ring_hi) {
         s.start1 = rt.start;
         s.n1 = npix;
         return s;
     }
-    const double x = PD_MUL(PD_SUB(p.cosr, PD_MUL(rt.z, p.z0)), p.xa);
+    const double x = PD_MUL(PD_SUB(cosr, PD_MUL(rt.z, p.z0)), p.xa);
     const double ysq = PD_SUB(rt.omz2, PD_MUL(x, x));
     if (!(ysq > 0.0)) return s;  // no intersection (HEALPix: dphi = 0, ring skipped)
     const float de = atan2f(sqrtf((float)ysq), (float)x);
@@ -349,8 +369,19 @@ __device__ __forceinline__ RingSpan fast_disc_ring(const Hpx& h, const DiscPlan&
     // |de - atan2(sqrt(ysq), x)| <= 3e-7 de (FP32 rounding of x, ysq and atan2f)
     const double m = fr * (4e-7 * (double)de) + 1e-9;
     const double flo = vlo - floor(vlo), fhi = vhi - floor(vhi);
-    if (!(de > 0.0f) || flo < m || flo > 1.0 - m || fhi < m || fhi > 1.0 - m)
-        return disc_ring(h, p, ring);
+    if (!(de > 0.0f) || flo < m || flo > 1.0 - m || fhi < m || fhi > 1.0 - m) {
+        DiscPlan d;
+        d.z0 = p.z0;
+        d.xa = p.xa;
+        d.cosr = cosr;
+        d.phi = p.phi;
+        d.ring_lo = p.ring_lo;
+        d.ring_hi = p.ring_hi;
+        d.full_lo = p.full_lo;
+        d.full_hi = p.full_hi;
+        d.all_sky = (p.flags & kPlanAllSky) != 0;
+        return disc_ring(h, d, ring);
+    }
     long long lo = (long long)floor(vlo) + 1;
     long long hi = (long long)floor(vhi);
     if (lo > hi) return s;
@@ -703,23 +734,90 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
     return swap ? 1.0f - a : a;
 }
 
-// A sample's per-sample geometry: its disc (the rings it touches and the
-// edge formula's constants), the boresight frame and the psi phasors.  Built
-// by make_plan, either inside the pair kernel (one warp per sample, every
-// lane redundantly) or beforehand by plan_kernel with one thread per sample:
-// it is FP64 work (about three hundred FP64 instructions), which GB300 runs
-// at a small fraction of its FP32 rate.  96 bytes.
-struct alignas(16) SamplePlan {
-    double z0, xa, phi;       // disc: cos(theta), 1 / sin(theta), longitude (disc_plan)
-    double phi_f, dec0;       // frame: longitude reduced mod 2 pi, latitude
-    float z0f, s0f;           // frame: sin and |cos| of the latitude
-    float sps, cps, c2p, s2p; // psi phasors (negated with the frame's flip)
-    int ring_lo, ring_hi;     // rings on the edge formula
-    int full_lo, full_hi;     // rings touched
-    int flags;                // kPlanBad: non-finite pointing; kPlanAllSky
+// Two pairs per lane and iteration in the nearest-lookup forward (1), or one (0).
+#ifndef PISCO_DUAL
+#define PISCO_DUAL 0
+#endif
+
+// One pair of the nearest lookup, up to its beam pixel and phasor.  use: the
+// pair contributes (in the disc, decided in FP32, beam pixel in the map);
+// fb: it is queued for the FP64 re-evaluation.
+struct PairG {
+    int pix, bp;
+    float c2, s2;
+    bool use, fb;
 };
-constexpr int kPlanBad = 1;
-constexpr int kPlanAllSky = 2;
+
+// The pair of batch position t (ring slot k of the batch W), branch-free
+// but for the series/sincosf choice of sin_versin; valid = t < total.  The
+// same FP32 operations, in the same order, as the one-pair loop of
+// sample_planned.
+__device__ __forceinline__ PairG pair_geom(const RingC* W, int k, int t, bool valid,
+                                           const Frame& F, const Beam& B, const Hpx& hs,
+                                           unsigned int* err)
+{
+    const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
+    const int4 R3 = *reinterpret_cast<const int4*>(&W[k].n1);
+    const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
+    const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
+    const int u = t - (R3.z - R3.w);
+    const bool first = u < R3.x;
+    const int pix = first ? R2.x + u : R2.y + (u - R3.x);
+    int kk = first ? R2.z + u : R2.w + (u - R3.x);
+    const int nr = R3.y;
+    if (kk >= (nr >> 1)) kk -= nr;
+    if (kk < -(nr >> 1)) kk += nr;
+    const bool bad = valid && (pix < 0 || pix >= hs.npix);
+    if (bad) record(err, kCheckSkyIndex);
+    const float dl = fmaf((float)kk, R0.y, R0.x);
+    float sn, h;
+    sin_versin(dl, sn, h);
+    const float u_e = R0.z * sn;
+    const float v_n = fmaf(R1.y, h, R0.w);
+    const float q = fmaf(R1.w, h, R1.x);
+    const float nb = F.s0 * sn;
+    const float db = fmaf(R1.z, h, -R0.w);
+    const float X = fmaf(u_e, F.sps, -v_n * F.cps);
+    const float Y = fmaf(u_e, F.cps, v_n * F.sps);
+    int qd;
+    float yy, xx;
+    if (Y >= 0.0f) {
+        if (X > 0.0f) { qd = 0; yy = Y; xx = X; }
+        else { qd = 1; yy = -X; xx = Y; }
+    } else {
+        if (X <= 0.0f) { qd = 2; yy = -Y; xx = -X; }
+        else { qd = 3; yy = X; xx = -Y; }
+    }
+    const float tp = quarter_turns(yy, xx);
+    const float r = B.rscale * (q * rsqrtf(q));
+    const float av = tp * r;
+    const float bv = (1.0f - tp) * r;
+    float fa, fbv, fc;
+    const int jp = split_floor(av, fa), jm = split_floor(bv, fbv);
+    const int ir = jp + jm + 1;
+    const float irf = __int_as_float(ir + kTwo23Bits) - kTwo23;
+    const float cv = tp * irf;
+    const int ipr = split_floor(cv, fc);
+    const float m = kMarginRel * (r + 1.0f);
+    const float mc = kMarginRel * (irf + 1.0f);
+    const bool near = q < kTinyQ || fa < m || 1.0f - fa < m || fbv < m || 1.0f - fbv < m ||
+                      fc < mc || 1.0f - fc < mc;
+    const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
+    PairG g;
+    g.pix = pix;
+    g.bp = bp;
+    g.fb = valid && !bad && near;
+    g.use = valid && !bad && !near && bp >= 0 && bp < B.npix;
+    const float wr = fmaf(db, v_n, -nb * u_e);
+    const float wi = fmaf(db, u_e, nb * v_n);
+    const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
+    const float er = fmaf(wr, wr, -wi * wi) * iw;
+    const float ei = 2.0f * wr * wi * iw;
+    g.c2 = fmaf(er, F.c2p, -ei * F.s2p);
+    g.s2 = fmaf(ei, F.c2p, er * F.s2p);
+    return g;
+}
+
 
 __device__ __forceinline__ SamplePlan make_plan(const Hpx& hs, const Beam& B, double ra,
                                                 double dec, double pa)
@@ -796,6 +894,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                                                unsigned long long& npairs)
 {
     constexpr bool kStaged = HasStage<Action>::value && !kBil && !kCalib;
+    constexpr bool kDual = PISCO_DUAL && Action::kSums && !kStaged && !kBil && !kCalib;
     RingC* W = S.r;
     const unsigned lt_mask = (1u << lane) - 1u;
     Frame F;
@@ -831,53 +930,66 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         Ps.f64 = o.f64;
         act.stash(Ps);
     }
+    static_assert(sizeof(SamplePlan) == 6 * sizeof(float4), "plan copy");
+    if (lane < 6)
+        reinterpret_cast<float4*>(&S.plan)[lane] = reinterpret_cast<const float4*>(&SP)[lane];
     __syncwarp();
     if constexpr (Action::kSums) act.reset();
-    DiscPlan P;
-    P.z0 = SP.z0;
-    P.xa = SP.xa;
-    P.cosr = B.cosr;
-    P.phi = SP.phi;
-    P.ring_lo = SP.ring_lo;
-    P.ring_hi = SP.ring_hi;
-    P.full_lo = SP.full_lo;
-    P.full_hi = SP.full_hi;
-    P.all_sky = (SP.flags & kPlanAllSky) != 0;
-    const double phi_f = SP.phi_f, dec0 = SP.dec0;
-    const float z0f = SP.z0f, s0f = SP.s0f;
-    F.s0 = s0f;
-    F.sps = SP.sps;
-    F.cps = SP.cps;
-    F.c2p = SP.c2p;
-    F.s2p = SP.s2p;
+    const SamplePlan& PL = S.plan;
+    // what the pair loop reads on every pair, in registers
+    F.s0 = PL.s0f;
+    F.sps = PL.sps;
+    F.cps = PL.cps;
+    F.c2p = PL.c2p;
+    F.s2p = PL.s2p;
+    const Beam& Bh = B;
+    // queue near-edge pairs (fb); redo them 32 at a time in FP64
+    [[maybe_unused]] auto enqueue = [&](bool fb, int pix) {
+        const unsigned mk = __ballot_sync(kFull, fb);
+        if (mk) {
+            if (fb) {
+                const int at = Qs.n + __popc(mk & lt_mask);
+                S.q[at] = pix;
+                S.qs[at] = (unsigned char)slot;
+            }
+            Qs.n += __popc(mk);
+            if (lane == 0) {
+                nfall += __popc(mk);
+                S.p[slot].left += __popc(mk);
+            }
+            __syncwarp();
+            if (Qs.n >= 32) drain<kBil>(hs, 32, S, Qs, lane, err, act);
+        }
+    };
 
-    for (long long r0 = P.full_lo; r0 <= P.full_hi; r0 += 32) {
+    for (long long r0 = PL.full_lo; r0 <= PL.full_hi; r0 += 32) {
         const long long ring = r0 + lane;
         int cnt = 0;
         RingC rc;
         rc.n1 = 0;
-        if (ring <= P.full_hi) {
+        if (ring <= PL.full_hi) {
             const RingT rt = rings[ring - 1];
-            const RingSpan sp = fast_disc_ring(hs, P, ring, rt);
+            const RingSpan sp = fast_disc_ring(hs, PL, B.cosr, ring, rt);
             cnt = (int)(sp.n1 + sp.n2);
             if (cnt) {
                 const double sh = (rt.npix2 & 1) ? 0.5 : 0.0;
+                const double phi_f = PL.phi_f;
                 const double jc = floor(phi_f * rt.fr - sh + 0.5);
                 rc.dc = (float)((jc + sh) * rt.dphi - phi_f);
                 rc.dphi = rt.dphif;
                 rc.si = rt.s;
                 // sin and 1 - cos of the latitude offset D: FP32 series at the
                 // rounded offset, first-order correction by its rounding error
-                const double dd = rt.dec - dec0;
+                const double dd = rt.dec - PL.dec0;
                 const float df = (float)dd;
                 const float de = (float)(dd - (double)df);
                 float sD, hD;
                 sin_versin(df, sD, hD);
                 rc.Di = fmaf(de, 1.0f - hD, sD);
                 rc.Ki = fmaf(de, sD, hD);
-                rc.Zs = rt.s * z0f;
-                rc.Wz = s0f * rt.zf;
-                rc.Pp = rt.s * s0f;
+                rc.Zs = rt.s * PL.z0f;
+                rc.Wz = PL.s0f * rt.zf;
+                rc.Pp = rt.s * PL.s0f;
                 rc.nr = rt.npix2 >> 1;
                 rc.b1 = (int)(sp.start1 - rt.start) - (int)jc;
                 rc.b2 = (int)(sp.start2 - rt.start) - (int)jc;
@@ -899,7 +1011,37 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         __syncwarp();
         if (lane == 0) npairs += (unsigned long long)total;
         int k = 0;  // lane slot (ring) owning the current pair; only moves forward
-        const int iters = (total + 31) >> 5;
+        if constexpr (kDual) {
+            // two pairs per lane and iteration, t and t + 32: their geometry
+            // is branch-free up to the loads, so the two dependency chains
+            // interleave; sums and queue entries keep the one-pair order
+            const int iters2 = (total + 63) >> 6;
+            for (int it = 0; it < iters2; ++it) {
+                const int t0 = (it << 6) + lane, t1 = t0 + 32;
+                if (t0 < total)
+                    while (W[k].incl <= t0) ++k;
+                const int k0 = k;
+                if (t1 < total)
+                    while (W[k].incl <= t1) ++k;
+                const PairG g0 = pair_geom(W, k0, t0, t0 < total, F, Bh, hs, err);
+                const PairG g1 = pair_geom(W, k, t1, t1 < total, F, Bh, hs, err);
+                float4 S0, S1;
+                F8 B0, B1;
+                if (g0.use) {
+                    S0 = act.fetch(g0.pix);
+                    B0 = load_beam(Bh.beam + g0.bp);
+                }
+                if (g1.use) {
+                    S1 = act.fetch(g1.pix);
+                    B1 = load_beam(Bh.beam + g1.bp);
+                }
+                if (g0.use) act.pair(g0.pix, S0, B0, g0.bp, g0.c2, g0.s2);
+                enqueue(g0.fb, g0.pix);
+                if (g1.use) act.pair(g1.pix, S1, B1, g1.bp, g1.c2, g1.s2);
+                enqueue(g1.fb, g1.pix);
+            }
+        }
+        const int iters = kDual ? 0 : (total + 31) >> 5;
         // staged action: the reads of iteration it are copied while the
         // geometry of iteration it + 1 runs, and summed after it, so each
         // lane's sums keep their order
@@ -952,7 +1094,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                         else { qd = 3; yy = X; xx = -Y; }
                     }
                     const float tp = quarter_turns(yy, xx);
-                    const float r = B.rscale * (q * rsqrtf(q));
+                    const float r = Bh.rscale * (q * rsqrtf(q));
                     // exp(2i (beta + alpha)) = w^2 / |w|^2, w = (db + i nb)(v + i u),
                     // then rotated by exp(2i psi)
                     auto phasor = [&](float& c2, float& s2) {
@@ -968,7 +1110,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                         fb = q < kTinyQ;
                         int px[4];
                         float w[4];
-                        if (!fb && stencil_f32(B, qd, tp, r, px, w)) {
+                        if (!fb && stencil_f32(Bh, qd, tp, r, px, w)) {
                             float c2, s2;
                             phasor(c2, s2);
                             act.pair_stencil(pix, act.fetch(pix), px, w, c2, s2);
@@ -978,7 +1120,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                     } else if constexpr (kBil) {
                         fb = q < kTinyQ;
                         F8 Bv;
-                        if (!fb && bilinear_f32(B, qd, tp, r, Bv)) {
+                        if (!fb && bilinear_f32(Bh, qd, tp, r, Bv)) {
                             float c2, s2;
                             phasor(c2, s2);
                             act.pair(pix, act.fetch(pix), Bv, -1, c2, s2);
@@ -1016,7 +1158,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                             (void)pair_beam_pixel(hs, hb, pix, F.ra, F.dec, F.psi, &rho, &sig, &chi);
                             const double tt = fmodulo(sig * kInvHalfPi, 4.0);
                             const double tpd = tt - floor(tt);
-                            const double rd = (double)B.nside * sqrt(3.0 * (1.0 - cos(rho)));
+                            const double rd = (double)Bh.nside * sqrt(3.0 * (1.0 - cos(rho)));
                             const double e1 = fabs(av - tpd * rd) / (r + 1.0);
                             const double e2 = fabs(bv - (1.0 - tpd) * rd) / (r + 1.0);
                             const double e3 = fabs(cv - tpd * (double)ir) / ((double)ir + 1.0);
@@ -1024,16 +1166,16 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                         }
                         if (!fb) {
                             const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
-                            if (bp >= 0 && bp < B.npix) {
+                            if (bp >= 0 && bp < Bh.npix) {
                                 float c2, s2;
                                 phasor(c2, s2);
                                 if constexpr (kStaged) {
-                                    act.issue(it & 1, lane, pix, B.beam + bp);
+                                    act.issue(it & 1, lane, pix, Bh.beam + bp);
                                     pnow = true;
                                     c2now = c2;
                                     s2now = s2;
                                 } else {
-                                    act.pair(pix, act.fetch(pix), load_beam(B.beam + bp), bp, c2,
+                                    act.pair(pix, act.fetch(pix), load_beam(Bh.beam + bp), bp, c2,
                                              s2);
                                 }
                             } else if constexpr (HasOutside<Action>::value) {
