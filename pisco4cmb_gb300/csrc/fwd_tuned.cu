@@ -50,10 +50,7 @@ __global__ void __launch_bounds__(kTW * 32, fwd_warps_per_sm<kCalib, kBil, kPlan
     tuned_kernel(FwdArgs a, float* calib, const tuned::SamplePlan* __restrict__ plans,
                  long long pos0, long long pos1)
 {
-    // the nearest lookup stages its sky and beam reads (tuned::StagedGather)
-    constexpr bool kStage = !kBil && !kCalib && PISCO_STAGE != 0;
     __shared__ tuned::WarpSmem sm[kTW];
-    __shared__ float4 stg[kStage ? kTW * tuned::kStageF4 : 1];
     const int lane = threadIdx.x & 31;
     tuned::WarpSmem& S = sm[threadIdx.x >> 5];
     // The nearest lookup keeps the grids' and the beam's descriptors in
@@ -82,9 +79,8 @@ __global__ void __launch_bounds__(kTW * 32, fwd_warps_per_sm<kCalib, kBil, kPlan
     const long long nw = (long long)gridDim.x * kTW;
     unsigned long long nfall = 0, npairs = 0;
     float cmax = 0.0f;
-    std::conditional_t<kStage, tuned::StagedGather, tuned::Gather> g;
+    tuned::Gather g;
     g.sky = a.sky32;
-    if constexpr (kStage) g.stage = stg + (threadIdx.x >> 5) * tuned::kStageF4;
     tuned::Queue Q{0, 0};
     for (long long i = pos0 + gw; i < pos1; i += nw) {
         const long long j = a.order ? (long long)a.order[i] : i;  // sample of position i

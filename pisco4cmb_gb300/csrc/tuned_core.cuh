@@ -88,12 +88,6 @@ template <class A, class = void>
 struct HasOutside : std::false_type {};
 template <class A>
 struct HasOutside<A, std::void_t<decltype(&A::outside)>> : std::true_type {};
-// Does the action stage its per-pair reads with asynchronous copies
-// (issue / consume, below)?
-template <class A, class = void>
-struct HasStage : std::false_type {};
-template <class A>
-struct HasStage<A, std::void_t<decltype(&A::issue)>> : std::true_type {};
 // Decisions whose FP32 value lies within kMarginRel * (value + 1) of an
 // integer are redone in FP64 (about 20 FP32 ulps).  The observed worst case
 // over a workload is measured by pisco_tuned_calibrate and must stay well
@@ -261,29 +255,6 @@ __device__ __forceinline__ float rcp_approx(float x)
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
-}
-
-// 16-byte asynchronous copies global -> this thread's shared memory
-// (cp.async, sm_80 and later): .cg caches in L2 only, .ca in L1 too.  A
-// thread sees the data after its own cp.async.wait_group.
-__device__ __forceinline__ void cp_async_cg16(void* smem, const void* gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_ca16(void* smem, const void* gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit()
-{
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // One beam pixel, both detectors (32 bytes, one sector): a single 256-bit
@@ -734,91 +705,6 @@ __device__ __forceinline__ float quarter_turns(float y, float x)
     return swap ? 1.0f - a : a;
 }
 
-// Two pairs per lane and iteration in the nearest-lookup forward (1), or one (0).
-#ifndef PISCO_DUAL
-#define PISCO_DUAL 0
-#endif
-
-// One pair of the nearest lookup, up to its beam pixel and phasor.  use: the
-// pair contributes (in the disc, decided in FP32, beam pixel in the map);
-// fb: it is queued for the FP64 re-evaluation.
-struct PairG {
-    int pix, bp;
-    float c2, s2;
-    bool use, fb;
-};
-
-// The pair of batch position t (ring slot k of the batch W), branch-free
-// but for the series/sincosf choice of sin_versin; valid = t < total.  The
-// same FP32 operations, in the same order, as the one-pair loop of
-// sample_planned.
-__device__ __forceinline__ PairG pair_geom(const RingC* W, int k, int t, bool valid,
-                                           const Frame& F, const Beam& B, const Hpx& hs,
-                                           unsigned int* err)
-{
-    const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
-    const int4 R3 = *reinterpret_cast<const int4*>(&W[k].n1);
-    const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
-    const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
-    const int u = t - (R3.z - R3.w);
-    const bool first = u < R3.x;
-    const int pix = first ? R2.x + u : R2.y + (u - R3.x);
-    int kk = first ? R2.z + u : R2.w + (u - R3.x);
-    const int nr = R3.y;
-    if (kk >= (nr >> 1)) kk -= nr;
-    if (kk < -(nr >> 1)) kk += nr;
-    const bool bad = valid && (pix < 0 || pix >= hs.npix);
-    if (bad) record(err, kCheckSkyIndex);
-    const float dl = fmaf((float)kk, R0.y, R0.x);
-    float sn, h;
-    sin_versin(dl, sn, h);
-    const float u_e = R0.z * sn;
-    const float v_n = fmaf(R1.y, h, R0.w);
-    const float q = fmaf(R1.w, h, R1.x);
-    const float nb = F.s0 * sn;
-    const float db = fmaf(R1.z, h, -R0.w);
-    const float X = fmaf(u_e, F.sps, -v_n * F.cps);
-    const float Y = fmaf(u_e, F.cps, v_n * F.sps);
-    int qd;
-    float yy, xx;
-    if (Y >= 0.0f) {
-        if (X > 0.0f) { qd = 0; yy = Y; xx = X; }
-        else { qd = 1; yy = -X; xx = Y; }
-    } else {
-        if (X <= 0.0f) { qd = 2; yy = -Y; xx = -X; }
-        else { qd = 3; yy = X; xx = -Y; }
-    }
-    const float tp = quarter_turns(yy, xx);
-    const float r = B.rscale * (q * rsqrtf(q));
-    const float av = tp * r;
-    const float bv = (1.0f - tp) * r;
-    float fa, fbv, fc;
-    const int jp = split_floor(av, fa), jm = split_floor(bv, fbv);
-    const int ir = jp + jm + 1;
-    const float irf = __int_as_float(ir + kTwo23Bits) - kTwo23;
-    const float cv = tp * irf;
-    const int ipr = split_floor(cv, fc);
-    const float m = kMarginRel * (r + 1.0f);
-    const float mc = kMarginRel * (irf + 1.0f);
-    const bool near = q < kTinyQ || fa < m || 1.0f - fa < m || fbv < m || 1.0f - fbv < m ||
-                      fc < mc || 1.0f - fc < mc;
-    const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
-    PairG g;
-    g.pix = pix;
-    g.bp = bp;
-    g.fb = valid && !bad && near;
-    g.use = valid && !bad && !near && bp >= 0 && bp < B.npix;
-    const float wr = fmaf(db, v_n, -nb * u_e);
-    const float wi = fmaf(db, u_e, nb * v_n);
-    const float iw = rcp_approx(fmaf(wr, wr, wi * wi));
-    const float er = fmaf(wr, wr, -wi * wi) * iw;
-    const float ei = 2.0f * wr * wi * iw;
-    g.c2 = fmaf(er, F.c2p, -ei * F.s2p);
-    g.s2 = fmaf(ei, F.c2p, er * F.s2p);
-    return g;
-}
-
-
 __device__ __forceinline__ SamplePlan make_plan(const Hpx& hs, const Beam& B, double ra,
                                                 double dec, double pa)
 {
@@ -893,8 +779,6 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                                                unsigned long long& nfall, float& cmax,
                                                unsigned long long& npairs)
 {
-    constexpr bool kStaged = HasStage<Action>::value && !kBil && !kCalib;
-    constexpr bool kDual = PISCO_DUAL && Action::kSums && !kStaged && !kBil && !kCalib;
     RingC* W = S.r;
     const unsigned lt_mask = (1u << lane) - 1u;
     Frame F;
@@ -943,24 +827,6 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
     F.c2p = PL.c2p;
     F.s2p = PL.s2p;
     const Beam& Bh = B;
-    // queue near-edge pairs (fb); redo them 32 at a time in FP64
-    [[maybe_unused]] auto enqueue = [&](bool fb, int pix) {
-        const unsigned mk = __ballot_sync(kFull, fb);
-        if (mk) {
-            if (fb) {
-                const int at = Qs.n + __popc(mk & lt_mask);
-                S.q[at] = pix;
-                S.qs[at] = (unsigned char)slot;
-            }
-            Qs.n += __popc(mk);
-            if (lane == 0) {
-                nfall += __popc(mk);
-                S.p[slot].left += __popc(mk);
-            }
-            __syncwarp();
-            if (Qs.n >= 32) drain<kBil>(hs, 32, S, Qs, lane, err, act);
-        }
-    };
 
     for (long long r0 = PL.full_lo; r0 <= PL.full_hi; r0 += 32) {
         const long long ring = r0 + lane;
@@ -1011,48 +877,11 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         __syncwarp();
         if (lane == 0) npairs += (unsigned long long)total;
         int k = 0;  // lane slot (ring) owning the current pair; only moves forward
-        if constexpr (kDual) {
-            // two pairs per lane and iteration, t and t + 32: their geometry
-            // is branch-free up to the loads, so the two dependency chains
-            // interleave; sums and queue entries keep the one-pair order
-            const int iters2 = (total + 63) >> 6;
-            for (int it = 0; it < iters2; ++it) {
-                const int t0 = (it << 6) + lane, t1 = t0 + 32;
-                if (t0 < total)
-                    while (W[k].incl <= t0) ++k;
-                const int k0 = k;
-                if (t1 < total)
-                    while (W[k].incl <= t1) ++k;
-                const PairG g0 = pair_geom(W, k0, t0, t0 < total, F, Bh, hs, err);
-                const PairG g1 = pair_geom(W, k, t1, t1 < total, F, Bh, hs, err);
-                float4 S0, S1;
-                F8 B0, B1;
-                if (g0.use) {
-                    S0 = act.fetch(g0.pix);
-                    B0 = load_beam(Bh.beam + g0.bp);
-                }
-                if (g1.use) {
-                    S1 = act.fetch(g1.pix);
-                    B1 = load_beam(Bh.beam + g1.bp);
-                }
-                if (g0.use) act.pair(g0.pix, S0, B0, g0.bp, g0.c2, g0.s2);
-                enqueue(g0.fb, g0.pix);
-                if (g1.use) act.pair(g1.pix, S1, B1, g1.bp, g1.c2, g1.s2);
-                enqueue(g1.fb, g1.pix);
-            }
-        }
-        const int iters = kDual ? 0 : (total + 31) >> 5;
-        // staged action: the reads of iteration it are copied while the
-        // geometry of iteration it + 1 runs, and summed after it, so each
-        // lane's sums keep their order
-        [[maybe_unused]] bool pprev = false;
-        [[maybe_unused]] float c2prev = 0.0f, s2prev = 0.0f;
+        const int iters = (total + 31) >> 5;
         for (int it = 0; it < iters; ++it) {
             const int t = (it << 5) + lane;
             bool fb = false;
             int pix = 0;
-            [[maybe_unused]] bool pnow = false;
-            [[maybe_unused]] float c2now = 0.0f, s2now = 0.0f;
             if (t < total) {
                 while (W[k].incl <= t) ++k;
                 const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
@@ -1169,32 +998,13 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                             if (bp >= 0 && bp < Bh.npix) {
                                 float c2, s2;
                                 phasor(c2, s2);
-                                if constexpr (kStaged) {
-                                    act.issue(it & 1, lane, pix, Bh.beam + bp);
-                                    pnow = true;
-                                    c2now = c2;
-                                    s2now = s2;
-                                } else {
-                                    act.pair(pix, act.fetch(pix), load_beam(Bh.beam + bp), bp, c2,
-                                             s2);
-                                }
+                                act.pair(pix, act.fetch(pix), load_beam(Bh.beam + bp), bp, c2, s2);
                             } else if constexpr (HasOutside<Action>::value) {
                                 act.outside(pix, bp);
                             }
                         }
                     }
                 }
-            }
-            if constexpr (kStaged) {
-                cp_async_commit();
-                if (it > 0) {
-                    cp_async_wait<1>();
-                    if (pprev) act.consume((it - 1) & 1, lane, c2prev, s2prev);
-                }
-                act.advance();
-                pprev = pnow;
-                c2prev = c2now;
-                s2prev = s2now;
             }
             // queue near-edge pairs; redo them 32 at a time in FP64
             const unsigned mk = __ballot_sync(kFull, fb);
@@ -1212,10 +1022,6 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                 __syncwarp();
                 if (Qs.n >= 32) drain<kBil>(hs, 32, S, Qs, lane, err, act);
             }
-        }
-        if constexpr (kStaged) {
-            cp_async_wait<0>();
-            if (pprev) act.consume((iters - 1) & 1, lane, c2prev, s2prev);
         }
         __syncwarp();
     }
@@ -1286,51 +1092,6 @@ struct Gather {
             a += __shfl_xor_sync(kFull, a, o);
             b += __shfl_xor_sync(kFull, b, o);
         }
-    }
-};
-
-// Forward action with the sky and beam reads staged through this warp's
-// shared memory by asynchronous copies (two buffers: the pair of iteration
-// it is copied while iteration it + 1 computes its geometry; TOD
-// bit-identical).  PISCO_STAGE 1: sky and beam copied; 2: beam copied, sky
-// loaded into registers; 0 (default): not staged.  Measured on the c2
-// forward (2M samples): 194.2 ms staged, 193.2 ms beam only, against
-// 174.9 ms unstaged -- the three copies, the wait and the three shared-memory
-// reads per pair cost more issue slots than the hidden L2 latency saves
-// (the same with 8 in-flight samples per warp, which keeps the block's
-// shared memory, and so L1, at its unstaged size: 194.0 / 194.3 ms).
-#ifndef PISCO_STAGE
-#define PISCO_STAGE 0
-#endif
-constexpr int kStageRows = PISCO_STAGE == 2 ? 2 : 3;
-// float4 per warp: [buffer][row: beam a, beam b, sky][lane]
-constexpr int kStageF4 = 2 * kStageRows * 32;
-
-struct StagedGather : Gather {
-    float4* stage;  // this warp's kStageF4 float4
-    float4 sk_cur, sk_prev;
-    __device__ __forceinline__ void issue(int buf, int lane, int pix, const F8* bp)
-    {
-        float4* d = stage + buf * (kStageRows * 32) + lane;
-        cp_async_cg16(d, &bp->a);
-        cp_async_cg16(d + 32, &bp->b);
-        if constexpr (kStageRows == 3) cp_async_ca16(d + 64, &sky[pix]);
-        else sk_cur = __ldg(&sky[pix]);
-    }
-    __device__ __forceinline__ void consume(int buf, int lane, float c2, float s2)
-    {
-        const float4* d = stage + buf * (kStageRows * 32) + lane;
-        F8 Bv;
-        Bv.a = d[0];
-        Bv.b = d[32];
-        float4 Sv;
-        if constexpr (kStageRows == 3) Sv = d[64];
-        else Sv = sk_prev;
-        pair(0, Sv, Bv, 0, c2, s2);
-    }
-    __device__ __forceinline__ void advance()
-    {
-        if constexpr (kStageRows == 2) sk_prev = sk_cur;
     }
 };
 
