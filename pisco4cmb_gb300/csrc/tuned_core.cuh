@@ -248,6 +248,14 @@ __device__ __forceinline__ int split_floor(float x, float& f)
     return __float_as_int(t) - kTwo23Bits;
 }
 
+// (float)k for |k| < 2^22 by FP32 addition: 1.5 * 2^23 + k lies in
+// [2^23, 2^24), where floats are the integers and their bits are linear in
+// the value, so no conversion instruction is needed (the same value).
+__device__ __forceinline__ float small_int_to_float(int k)
+{
+    return __int_as_float(0x4B400000 + k) - 12582912.0f;
+}
+
 // 1/x by the MUFU reciprocal approximation (relative error below 2^-22);
 // used only for values, never for an index decision.
 __device__ __forceinline__ float rcp_approx(float x)
@@ -835,7 +843,14 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         rc.n1 = 0;
         if (ring <= PL.full_hi) {
             const RingT rt = rings[ring - 1];
-            const RingSpan sp = fast_disc_ring(hs, PL, B.cosr, ring, rt);
+            RingSpan sp = fast_disc_ring(hs, PL, B.cosr, ring, rt);
+            // every pixel of the ring's range(s) must lie in the sky map:
+            // checked here, once per ring, instead of once per pair
+            if (sp.start1 < 0 || sp.start1 + sp.n1 > hs.npix ||
+                (sp.n2 > 0 && (sp.start2 < 0 || sp.start2 + sp.n2 > hs.npix))) {
+                record(err, kCheckSkyIndex);
+                sp = RingSpan{0, 0, 0, 0};
+            }
             cnt = (int)(sp.n1 + sp.n2);
             if (cnt) {
                 const double sh = (rt.npix2 & 1) ? 0.5 : 0.0;
@@ -898,12 +913,10 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                 const int nr = R3.y;
                 if (kk >= (nr >> 1)) kk -= nr;
                 if (kk < -(nr >> 1)) kk += nr;
-                if (pix < 0 || pix >= hs.npix) {
-                    record(err, kCheckSkyIndex);
-                } else {
+                {
                     const float4 R0 = *reinterpret_cast<const float4*>(&W[k].dc);
                     const float4 R1 = *reinterpret_cast<const float4*>(&W[k].Ki);
-                    const float dl = fmaf((float)kk, R0.y, R0.x);
+                    const float dl = fmaf(small_int_to_float(kk), R0.y, R0.x);
                     float sn, h;
                     sin_versin(dl, sn, h);
                     const float u_e = R0.z * sn;
