@@ -102,8 +102,8 @@ constexpr float kTinyQ = 4.0e-12f;
 struct alignas(16) RingC {
     float dc, dphi, si, Di;  // anchor offset, pixel spacing, s, sin(dec - dec0)
     float Ki, Zs, Wz, Pp;    // 1 - cos(dec - dec0), s z0, s0 z, s s0
-    int s1, s2, b1, b2;      // range starts, anchor offsets of the ranges
-    int n1, nr, incl, cnt;   // first range length, ring pixels, inclusive scan, pixels
+    int s1, s2, b1, b2;      // range starts, anchor offsets of the ranges (second: minus n1)
+    int n1, nr, incl, base;  // first range length, ring pixels, inclusive scan, first index
 };
 
 // Samples in flight per warp (a sample keeps its slot until its queued
@@ -873,11 +873,11 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                 rc.Pp = rt.s * PL.s0f;
                 rc.nr = rt.npix2 >> 1;
                 rc.b1 = (int)(sp.start1 - rt.start) - (int)jc;
-                rc.b2 = (int)(sp.start2 - rt.start) - (int)jc;
+                rc.b2 = (int)(sp.start2 - rt.start) - (int)jc - (int)sp.n1;
             }
             rc.n1 = (int)sp.n1;
             rc.s1 = (int)sp.start1;
-            rc.s2 = (int)sp.start2;
+            rc.s2 = (int)sp.start2 - (int)sp.n1;
         }
         int incl = cnt;
 #pragma unroll
@@ -887,7 +887,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         }
         const int total = __shfl_sync(kFull, incl, 31);
         rc.incl = incl;
-        rc.cnt = cnt;
+        rc.base = incl - cnt;
         W[lane] = rc;
         __syncwarp();
         if (lane == 0) npairs += (unsigned long long)total;
@@ -901,15 +901,10 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                 while (W[k].incl <= t) ++k;
                 const int4 R2 = *reinterpret_cast<const int4*>(&W[k].s1);
                 const int4 R3 = *reinterpret_cast<const int4*>(&W[k].n1);
-                const int u = t - (R3.z - R3.w);
-                int kk;
-                if (u < R3.x) {
-                    pix = R2.x + u;
-                    kk = R2.z + u;
-                } else {
-                    pix = R2.y + (u - R3.x);
-                    kk = R2.w + (u - R3.x);
-                }
+                const int u = t - R3.w;  // index within the ring's pixels
+                const bool first = u < R3.x;
+                pix = (first ? R2.x : R2.y) + u;
+                int kk = (first ? R2.z : R2.w) + u;
                 const int nr = R3.y;
                 if (kk >= (nr >> 1)) kk -= nr;
                 if (kk < -(nr >> 1)) kk += nr;
@@ -1008,7 +1003,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
                         }
                         if (!fb) {
                             const int bp = 2 * ir * (ir - 1) + qd * ir + ipr;
-                            if (bp >= 0 && bp < Bh.npix) {
+                            if ((unsigned)bp < (unsigned)Bh.npix) {  // 0 <= bp < npix
                                 float c2, s2;
                                 phasor(c2, s2);
                                 act.pair(pix, act.fetch(pix), load_beam(Bh.beam + bp), bp, c2, s2);
