@@ -25,7 +25,9 @@ namespace {
 // whose discs overlap, so their sky reads share L1.  Its 169 KB of per-warp
 // shared state is a static allocation, which sm_103a allows beyond 48 KB.
 // The bilinear lookup, which needs more registers per pair, runs 8 x 2 with
-// its descriptors in registers (296.3 ms; from shared memory 374.1 ms).
+// its descriptors in registers (296.3 ms; from shared memory 374.1 ms).  For
+// the nearest lookup the beam's descriptor in registers (its pointer and size
+// then come from the kernel parameters) is slower: 133.4 against 120.4 ms.
 #ifndef PISCO_FWD_WARPS
 #define PISCO_FWD_WARPS 32
 #endif

@@ -136,6 +136,7 @@ struct alignas(16) Pend {
 struct alignas(16) SamplePlan {
     double z0, xa, phi;       // disc: cos(theta), 1 / sin(theta), longitude (disc_plan)
     double phi_f, dec0;       // frame: longitude reduced mod 2 pi, latitude
+    double cosr;              // disc: cos(radius) (the beam's, as evaluated on the device)
     float z0f, s0f;           // frame: sin and |cos| of the latitude
     float sps, cps, c2p, s2p; // psi phasors (negated with the frame's flip)
     int ring_lo, ring_hi;     // rings on the edge formula
@@ -764,6 +765,7 @@ __device__ __forceinline__ SamplePlan make_plan(const Hpx& hs, const Beam& B, do
     sp.z0 = P.z0;
     sp.xa = P.xa;
     sp.phi = P.phi;
+    sp.cosr = B.cosr;
     sp.ring_lo = (int)P.ring_lo;
     sp.ring_hi = (int)P.ring_hi;
     sp.full_lo = (int)P.full_lo;
@@ -843,7 +845,7 @@ __device__ __forceinline__ void sample_planned(const SamplePlan& SP, const Hpx& 
         rc.n1 = 0;
         if (ring <= PL.full_hi) {
             const RingT rt = rings[ring - 1];
-            RingSpan sp = fast_disc_ring(hs, PL, B.cosr, ring, rt);
+            RingSpan sp = fast_disc_ring(hs, PL, PL.cosr, ring, rt);
             // every pixel of the ring's range(s) must lie in the sky map:
             // checked here, once per ring, instead of once per pair
             if (sp.start1 < 0 || sp.start1 + sp.n1 > hs.npix ||
