@@ -1,6 +1,12 @@
 // tuned_core.cuh -- per-sample body of the TUNED geometry, shared by the
 // single-detector forward (fwd_tuned.cu), the batched multi-detector forward
-// (fwd_batched.cu) and the adjoint (adjoint.cu).
+// (fwd_batched.cu) and the adjoint (adjoint_kernels.cuh).
+//
+// A sample's FP64 set-up -- its disc plan, boresight frame and psi phasors
+// (SamplePlan, make_plan) -- is built beforehand by a plan kernel with one
+// thread per sample, or by the warp itself; the warp keeps it in its shared
+// memory (WarpSmem::plan), so the pair loop's registers hold only the pair
+// geometry (the kernels run 32 warps per SM at 64 registers).
 //
 // For one sample, a warp evaluates the HEALPix query_disc rings, one ring per
 // lane, rounds per-ring small-offset constants to FP32 once, and strides the
@@ -67,9 +73,10 @@
 #include "hpx.cuh"
 #include "internal.h"
 
-// Warps per block of the kernels built on this core, and the minimum number
-// of resident blocks per SM requested from the compiler (which caps their
-// registers at 65536 / (32 x warps x blocks)).
+// Warps per block of the adjoint's and the diagnostics' kernels, and the
+// minimum number of resident blocks per SM requested from the compiler (which
+// caps their registers at 65536 / (32 x warps x blocks)); the adjoint's
+// planned nearest-lookup instances take 4 blocks (adjoint_kernels.cuh).
 #ifndef PISCO_TUNED_WARPS
 #define PISCO_TUNED_WARPS 8
 #endif
