@@ -264,6 +264,12 @@ __device__ __forceinline__ float small_int_to_float(int k)
     return __int_as_float(0x4B400000 + k) - 12582912.0f;
 }
 
+// The inverse for an integer-valued float f, |f| < 2^22 (exact, no conversion).
+__device__ __forceinline__ int small_float_to_int(float f)
+{
+    return __float_as_int(f + 12582912.0f) - 0x4B400000;
+}
+
 // 1/x by the MUFU reciprocal approximation (relative error below 2^-22);
 // used only for values, never for an index decision.
 __device__ __forceinline__ float rcp_approx(float x)
@@ -477,13 +483,14 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
 {
     const float c = 1.0f / (2.4494897427831781f * (float)B.nside);  // 1 / (sqrt(6) nside)
     const float c2 = c * c;
-    const int k = (int)r;  // ring above (0 above the first ring)
+    float kfr;
+    const int k = split_floor(r, kfr);  // ring above (0 above the first ring); r >= 0
     // longitude interpolation on ring i: pixels start + i1, start + i1 + 1
     auto ring = [&](int i, int& p1, int& p2, float& w1, float& w2) {
-        const float t = fmaf(tp, (float)i, -0.5f);
+        const float t = fmaf(tp, small_int_to_float(i), -0.5f);
         const float fl = floorf(t);
         const float f = t - fl;
-        int i1 = (int)fl + qd * i, i2 = i1 + 1;
+        int i1 = small_float_to_int(fl) + qd * i, i2 = i1 + 1;
         const int np = 4 * i;
         if (i1 < 0) i1 += np;
         if (i2 >= np) i2 -= np;
@@ -517,7 +524,7 @@ __device__ __forceinline__ bool bilinear_f32(const Beam& B, int qd, float tp, fl
         add(p1, fmaf(w1, wt, f));
         add(p2, fmaf(w2, wt, f));
     } else {
-        const float kf = (float)k;
+        const float kf = small_int_to_float(k);
         const float wt = wdiv((r - kf) * asin_slope(r, kf, c2), asin_slope(kf + 1.0f, kf, c2));
         ring(k, p1, p2, w1, w2);
         add(p1, w1 * (1.0f - wt));
@@ -541,12 +548,13 @@ __device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, flo
 {
     const float c = 1.0f / (2.4494897427831781f * (float)B.nside);
     const float c2 = c * c;
-    const int k = (int)r;
+    float kfr;
+    const int k = split_floor(r, kfr);  // r >= 0
     auto ring = [&](int i, int& p1, int& p2, float& w1, float& w2) {
-        const float t = fmaf(tp, (float)i, -0.5f);
+        const float t = fmaf(tp, small_int_to_float(i), -0.5f);
         const float fl = floorf(t);
         const float f = t - fl;
-        int i1 = (int)fl + qd * i, i2 = i1 + 1;
+        int i1 = small_float_to_int(fl) + qd * i, i2 = i1 + 1;
         const int np = 4 * i;
         if (i1 < 0) i1 += np;
         if (i2 >= np) i2 -= np;
@@ -569,7 +577,7 @@ __device__ __forceinline__ bool stencil_f32(const Beam& B, int qd, float tp, flo
     } else {
         ring(k, px[0], px[1], w[0], w[1]);
         ring(k + 1, px[2], px[3], w[2], w[3]);
-        const float kf = (float)k;
+        const float kf = small_int_to_float(k);
         const float wt = wdiv((r - kf) * asin_slope(r, kf, c2), asin_slope(kf + 1.0f, kf, c2));
         w[0] *= 1.0f - wt;
         w[1] *= 1.0f - wt;
