@@ -89,9 +89,20 @@ pisco_status pisco_ctx::ensure(void** p, size_t* cap, size_t bytes, const char* 
     pisco_ctx* c = this;
     if (*cap >= bytes && *p) return PISCO_OK;
     size_t grow = bytes - (*p ? *cap : 0);
-    if (cfg.maxMemUsage && mem_used + grow > cfg.maxMemUsage)
-        return fail(this, PISCO_ERR_OUT_OF_MEMORY,
-                    std::string(what) + ": maxMemUsage of the RunConfig exceeded");
+    if (cfg.maxMemUsage && mem_used + grow > cfg.maxMemUsage) {
+        // the sample-plan scratch yields to every other buffer: freed when
+        // that makes room (the forward then plans again within what is left)
+        if (p != &plans && plans && mem_used - plans_cap + grow <= cfg.maxMemUsage) {
+            CK(cudaDeviceSynchronize(), "sync before freeing the plan scratch");
+            cudaFree(plans);
+            mem_used -= plans_cap;
+            plans = nullptr;
+            plans_cap = 0;
+        } else {
+            return fail(this, PISCO_ERR_OUT_OF_MEMORY,
+                        std::string(what) + ": maxMemUsage of the RunConfig exceeded");
+        }
+    }
     if (*p) {
         CK(cudaStreamSynchronize(stream), "sync before realloc");
         cudaFree(*p);

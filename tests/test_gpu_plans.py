@@ -127,3 +127,37 @@ def test_forwards_on_two_streams_share_the_plan_scratch(gpu):
         assert np.array_equal(a.cpu().numpy(), ref[0][b0:b0 + m], equal_nan=True)
         assert np.array_equal(b.cpu().numpy(), ref[1][b0:b0 + m], equal_nan=True)
     conv.close()
+
+
+def test_plan_scratch_yields_to_inputs_under_max_mem_usage(gpu):
+    """Under a maxMemUsage limit the plan scratch gives way to a larger input:
+    the input is accepted, the next forward plans within what is left (here
+    in chunks), and its TOD equals that of a context without a limit."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, RunConfig, Sky
+
+    free = GPUConvolver(form="tuned")
+    n = _setup(free)
+    before = free.memory_used()
+    free.close()
+    conv = GPUConvolver(RunConfig(maxMemUsage=before + PLAN_BYTES * n, ptgPerConv=4096),
+                        form="tuned")
+    _setup(conv)
+    _tod(conv, n, False)
+    assert conv.memory_used() == before + PLAN_BYTES * n  # the scratch filled the room
+    # a larger sky: 12 * 160^2 * 16 B, 1.8 MB more than nside 128, fits only without the scratch
+    rng = np.random.default_rng(21)
+    nss = 160
+    sky = rng.normal(size=(3, 12 * nss * nss)).astype(np.float32)
+    conv.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    assert conv.memory_used() <= before + PLAN_BYTES * n
+    a, b = _tod(conv, n, False)
+    assert conv.memory_used() <= before + PLAN_BYTES * n
+    conv.close()
+    ref = GPUConvolver(form="tuned")
+    _setup(ref)
+    ref.update_sky(Sky(nss, sky[0], sky[1], sky[2], None))
+    ra_, rb_ = _tod(ref, n, False)
+    ref.close()
+    assert np.array_equal(a, ra_, equal_nan=True) and np.array_equal(b, rb_, equal_nan=True)
