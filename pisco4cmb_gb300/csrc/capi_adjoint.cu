@@ -237,11 +237,15 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
         a.ceps_q = pp->cq;
     }
     // the samples' plans, if the whole range fits the scratch (the launch is
-    // not split: the parameter gradient's per-warp rows cover one launch)
-    void* plans = nullptr;
-    long long plan_cap = 0;
-    if (n > 0) c->plan_scratch(n, s, &plans, &plan_cap, kAdjointPlans);
-    if (plan_cap >= n) a.plans = static_cast<tuned::SamplePlan*>(plans);
+    // not split: the parameter gradient's per-warp rows cover one launch);
+    // taken after every other buffer of the call, which may free the scratch
+    auto take_plans = [&]() {
+        void* plans = nullptr;
+        long long plan_cap = 0;
+        a.plans = nullptr;
+        if (n > 0) c->plan_scratch(n, s, &plans, &plan_cap, kAdjointPlans);
+        if (plans && plan_cap >= n) a.plans = static_cast<tuned::SamplePlan*>(plans);
+    };
     int nwarps = 0;
     CK(cudaMemsetAsync(c->d_fallbacks, 0, sizeof(unsigned long long), s), "reset fallbacks");
     if (!deterministic) {
@@ -268,6 +272,7 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
         }
         a.gsky32 = gs;
         a.gbeam32 = gbm;
+        take_plans();
         if (n > 0) CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);
         if (a.plans) c->plans_used(s);
@@ -316,6 +321,7 @@ pisco_status adjoint_core(pisco_ctx* c, long begin, long n, const void* d_ga, co
             CK(cudaMemsetAsync(c->adj_beam_fx, 0, 8 * nbeam, s), "zero beam accumulator");
             a.gbeam_fx = c->adj_beam_fx;
         }
+        take_plans();
         if (n > 0 && (a.sky_scale > 0.0 || a.beam_scale > 0.0 || pp))
             CK(launch_adjoint(a, c->sm_count, s, &nwarps), "adjoint launch");
         if (a.order) c->order_used(s);

@@ -191,14 +191,18 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
     if (st != PISCO_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     // every detector's sample plans in one scratch (planned launch), if it
-    // fits: the graph below holds its address
+    // fits: the graph below holds its address, so the key names it
     long long total = 0;
     for (int d = 0; d < ndet; ++d) total += dets[d].nsamples;
     void* plans = nullptr;
-    long long plan_cap = 0;
-    if (total > 0) c->plan_scratch(total, s, &plans, &plan_cap, kBatchPlans);
-    if (plan_cap < total) plans = nullptr;
-    const std::string key = launch_key(c, dets, ndet, out_dtype, chunk, warps, plans);
+    auto take_plans = [&]() {
+        long long plan_cap = 0;
+        plans = nullptr;
+        if (total > 0) c->plan_scratch(total, s, &plans, &plan_cap, kBatchPlans);
+        if (plan_cap < total) plans = nullptr;
+    };
+    take_plans();
+    std::string key = launch_key(c, dets, ndet, out_dtype, chunk, warps, plans);
     if (!(c->graph_exec && key == c->graph_key)) {
         // the descriptors, items and orders below may still be read by the
         // previous launch (on another stream)
@@ -239,6 +243,10 @@ pisco_status pisco_forward_batched(pisco_ctx* c, const pisco_det_desc* dets, int
         size_t qcap = c->d_queue ? sizeof(unsigned int) : 0;
         if (st == PISCO_OK) st = c->ensure((void**)&c->d_queue, &qcap, sizeof(unsigned int), "batch queue");
         if (st != PISCO_OK) return st;
+        // the buffers above may have freed the plan scratch (it yields to
+        // them): take it again, after them, and key the graph on it
+        take_plans();
+        key = launch_key(c, dets, ndet, out_dtype, chunk, warps, plans);
         CK(cudaMemcpyAsync(c->d_dets, bd.data(), sizeof(BatchDet) * ndet, cudaMemcpyHostToDevice, c->stream),
            "descriptors H2D");
         if (!items.empty())

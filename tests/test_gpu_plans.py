@@ -161,3 +161,42 @@ def test_plan_scratch_yields_to_inputs_under_max_mem_usage(gpu):
     ra_, rb_ = _tod(ref, n, False)
     ref.close()
     assert np.array_equal(a, ra_, equal_nan=True) and np.array_equal(b, rb_, equal_nan=True)
+
+
+def test_adjoint_takes_its_plans_after_its_other_buffers(gpu):
+    """The DETERMINISTIC adjoint allocates its fixed-point sky accumulator in
+    the call; under a maxMemUsage limit that the forward's plan scratch has
+    filled, that allocation frees the scratch, and the adjoint must take its
+    plans only afterwards (here: no room for them, so its warps plan).  The
+    gradient equals that of a context without a limit, bit for bit."""
+    import torch
+
+    from pisco4cmb_gb300 import GPUConvolver, RunConfig
+
+    nss = 128
+    npix = 12 * nss * nss
+    free = GPUConvolver(form="tuned")
+    n = _setup(free, nss=nss)
+    before = free.memory_used()
+    rng = np.random.default_rng(4)
+    g = [torch.tensor(rng.normal(size=n), device="cuda") for _ in range(2)]
+
+    def adjoint(conv):
+        out = torch.zeros((npix, 4), dtype=torch.float64, device="cuda")
+        conv.adjoint_device(g[0].data_ptr(), g[1].data_ptr(), True, out.data_ptr(), 0, out_f64=True,
+                            deterministic=True, sky_iqu=True)
+        conv.sync()
+        return out.cpu().numpy()
+
+    want = adjoint(free)
+    free.close()
+    fx = 8 * 4 * npix  # the fixed-point sky accumulator
+    cap = before + fx + 3 * 256 * 8 + PLAN_BYTES * n - (1 << 20)
+    conv = GPUConvolver(RunConfig(maxMemUsage=cap, ptgPerConv=4096), form="tuned")
+    _setup(conv, nss=nss)
+    _tod(conv, n, False)
+    assert conv.memory_used() == before + PLAN_BYTES * n  # the forward's scratch is in place
+    got = adjoint(conv)
+    assert conv.memory_used() <= cap
+    conv.close()
+    assert np.array_equal(got, want)
