@@ -455,6 +455,8 @@ def run_gpu_arm(args, rank, world, local):
                          "kernel": "the forward step: plan_kernel + tuned_kernel",
                          "traffic": traffic,
                          "bytes_model": "48 B/pair x exact disc pairs + 32 B/sample",
+                         "note": ("the byte model counts the sky and beam gathers that L1 and L2 "
+                                  "serve; DRAM moves `traffic` bytes per pair-kernel launch"),
                          "l2": l2_line},
             "plain": {"value": plain_sps, "unit": "samples/s", "sample": m_plain,
                       "tuned_over_plain": value / world / plain_sps},
