@@ -159,9 +159,14 @@ struct ScatterBeam {
     __device__ __forceinline__ void add_beam(long long bp, const float v[8], float w) const
     {
         if (kFixed) {
+            // an integer add of 0 changes nothing: zero values (the V
+            // column of a sky without V, say) issue no atomic
             unsigned long long* p = gbeam_fx + 8 * bp;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) atomicAdd(p + k, Scatter<kFixed>::fx(v[k] * w, sbeam));
+            for (int k = 0; k < 8; ++k) {
+                const unsigned long long x = Scatter<kFixed>::fx(v[k] * w, sbeam);
+                if (x) atomicAdd(p + k, x);
+            }
         } else {
             float4* p = reinterpret_cast<float4*>(gbeam) + 2 * bp;
             atomicAdd(p, make_float4(v[0] * w, v[1] * w, v[2] * w, v[3] * w));
@@ -182,7 +187,10 @@ struct ScatterBeam {
         if (kFixed) {
             unsigned long long* p = gbeam_fx + 8 * bp;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) atomicAdd(p + k, Scatter<kFixed>::fx(v[k], sbeam));
+            for (int k = 0; k < 8; ++k) {
+                const unsigned long long x = Scatter<kFixed>::fx(v[k], sbeam);
+                if (x) atomicAdd(p + k, x);  // adding 0 changes nothing
+            }
         } else {
             float4* p = reinterpret_cast<float4*>(gbeam) + 2 * bp;
             atomicAdd(p, make_float4(v[0], v[1], v[2], v[3]));
