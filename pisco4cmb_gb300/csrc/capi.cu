@@ -195,6 +195,11 @@ void pisco_ctx::plan_scratch(long long n, cudaStream_t s, void** p, long long* c
     }
     const long long need = std::min(n, kMinPlans);
     if (fit >= need && plans_cap < pisco::kSamplePlanBytes * (size_t)fit) {
+        // growing frees the old scratch: wait for its last reader, on any stream
+        if (plans && plan_event && cudaEventSynchronize(plan_event) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
         const std::string keep = error;
         if (ensure(&plans, &plans_cap, pisco::kSamplePlanBytes * (size_t)fit, "sample plans") !=
             PISCO_OK)
